@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""Benchmark of the multicanonical weight-estimation hot path on GB300.
+
+Metric (the benchmark spec): spin-flip attempts/ns at L=72, one GB300 against the
+host CPU.  One step = one iteration of the reference weight loop
+(muca_delta_multigpu.cu:374-477) on the workload of the L=72 configuration:
+16384 chains, therm = N = 5184 attempts then nup = N recorded attempts per
+chain (2 * 5184 * 16384 = 169.9 M attempts), followed by the FP64 trivial
+weight update on the device.  Spins start from the reference initialisation
+(muca_delta_multigpu.cu:340-354); all inputs are synthetic (no dataset).
+
+  value  device time of the K timed steps (CUDA events on the engine's
+         stream), L2 flushed (256 MiB write) before every timed step;
+  e2e    the same steps through the C ABI with host buffers: weights H2D
+         from pinned memory, sweep, update, weights + histogram D2H, timed
+         on the host clock;
+  roofline      HBM form: 1.5 algorithmic bytes per attempt (2-bit spins:
+                site read + write, 4 neighbour reads) over the sweep kernel's
+                event time, against the measured copy bandwidth;
+  roofline_int  the bound that applies (lattice resident in shared memory):
+                0.5 Philox4x32-7 blocks per attempt against the measured
+                Philox block rate of this GPU (muca_philox_peak);
+  cpu_baseline  the CPU oracle (the reference algorithm restated in C, one
+                chain per thread task, all host threads) on full steps.
+
+`--impl reference` times the reference's CPU algorithm (the oracle port: the
+reference CPU sources cannot be built on the GPU host) on the same workload.
+With N > 1 processes (torchrun), every rank runs its own shard as reference
+device `rank` (its own seeds), no collective on the data path: weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L_DEFAULT, CHAINS_DEFAULT = 72, 16384
+METRIC = "spin-flip attempts/ns at L=72 (1 GB300 vs host CPU)"
+ALG_BYTES_PER_ATTEMPT = 1.5     # 2-bit spins: read+write of the site, 4 neighbour reads
+PHILOX_BLOCKS_PER_ATTEMPT = 0.5  # two Philox4x32 blocks per four attempts
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--L", type=int, default=L_DEFAULT)
+    p.add_argument("--chains", type=int, default=CHAINS_DEFAULT)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-ref-gpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            t = [x.strip() for x in line.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                mx.append(float(t[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, t[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def profile_traffic():
+    """DRAM bytes per sweep launch from the committed ncu summary, if any."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json")))
+        return d
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_oracle_rate(L, chains, nthreads, min_seconds=4.0, max_reps=5):
+    """The reference algorithm on the host: full steps (therm=N, nup=N) of
+    `chains` chains with `nthreads` POSIX threads; returns (attempts/ns, sample)."""
+    import numpy as np
+    from oracle import orc
+    N = L * L
+    lat = orc.init_lattice(L, chains, orc.scheme_weight(0, 0))
+    ej, ed, _ = orc.energies(L, lat)
+    w32 = np.zeros(N + 1, np.float32)
+    done = 0
+    t_total = 0.0
+    reps = 0
+    while reps < max_reps and (t_total < min_seconds or reps < 1):
+        t0 = time.perf_counter()
+        orc.weight_sweep(L, lat, ej, ed, w32, reps, 100, N, N, nthreads=nthreads)
+        t_total += time.perf_counter() - t0
+        done += chains * 2 * N
+        reps += 1
+    return done / (t_total * 1e9), ("%d step(s) of %d chains x (therm N + nup N) at L=%d, %.1f s wall"
+                                    % (reps, chains, L, t_total))
+
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return 0
+    L, chains = args.L, args.chains
+    N = L * L
+    nthreads = os.cpu_count() or 1
+    import numpy as np
+    from oracle import orc
+    orc.build()
+    lat = orc.init_lattice(L, chains, orc.scheme_weight(0, 0))
+    ej, ed, _ = orc.energies(L, lat)
+    lnw = np.zeros(N + 1)
+    h = np.zeros(N + 1, np.uint64)
+    # a bounded sample of the workload per step: all chains when one step
+    # takes at most ~2 s on this host, fewer otherwise
+    t0 = time.perf_counter()
+    sub = min(chains, 1024)
+    orc.weight_sweep(L, lat[:sub], ej[:sub], ed[:sub], lnw.astype(np.float32), 0, 100, N, N, nthreads=nthreads)
+    per_chain = (time.perf_counter() - t0) / sub
+    sample = max(nthreads, min(chains, int(2.0 / max(per_chain, 1e-9))))
+    lat, ej, ed = lat[:sample].copy(), ej[:sample].copy(), ed[:sample].copy()
+    times = []
+    for k in range(args.warmup + args.steps):
+        h[:] = 0
+        t0 = time.perf_counter()
+        orc.weight_sweep(L, lat, ej, ed, lnw.astype(np.float32), k, 100, N, N, nthreads=nthreads, hist=h)
+        orc.lib().orc_update_trivial_gpu(h, N, lnw)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+    attempts = sample * 2 * N
+    v = attempts * len(times) / (sum(times) * 1e9)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "attempts/ns", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
+            "data": "synthetic (reference initial spins, zero initial weights)",
+            "config": {"workload": "weight-estimation iteration, L=%d, %d chains, therm=N, nup=N, trivial update"
+                                   % (L, chains), "L": L, "chains": chains, "chains_timed_per_step": sample},
+            "cpu_baseline": {"value": v, "unit": "attempts/ns", "cores": nthreads, "kind": "port",
+                             "sample": "%d of %d chains per step (therm N + nup N), %d steps" % (sample, chains,
+                                                                                               len(times))},
+            "e2e": {"value": v, "unit": "attempts/ns", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def ours_arm(args, ws, rank, local):
+    import numpy as np
+    import torch
+    import muca_gb300 as m
+    from muca_gb300 import build as b
+
+    b.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist_
+        dist_.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist = dist_
+    L, chains = args.L, args.chains
+    N = L * L
+    attempts_per_step = chains * 2 * N
+    stream = torch.cuda.Stream()
+    eng = m.Engine(L, nchains=chains, device=local, stream=stream.cuda_stream, dev_offset=rank)
+    eng.init_chains(m.INIT_WEIGHT, 0)
+    eng.set_weights(np.zeros(N + 1))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    k = 0
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        eng.sweep(k, 100, 1000, N, N)
+        eng.update_weights(m.UPDATE_TRIVIAL, wait=False)
+        k += 1
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    t_wall0 = time.perf_counter()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1, e2 = ev[i]
+        e0.record(stream)
+        eng.sweep(k, 100, 1000, N, N)
+        e1.record(stream)
+        eng.update_weights(m.UPDATE_TRIVIAL, wait=False)
+        e2.record(stream)
+        k += 1
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    sweep_ms = [a.elapsed_time(b_) for a, b_, _ in ev]
+    step_ms = [a.elapsed_time(c_) for a, _, c_ in ev]
+    t_dev = sum(step_ms) * 1e-3
+    # max over ranks
+    if dist is not None:
+        t = torch.tensor([t_dev, sum(sweep_ms) * 1e-3, t_wall], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_dev, t_sweep, t_wall = (float(x) for x in t.tolist())
+    else:
+        t_sweep = sum(sweep_ms) * 1e-3
+    value = ws * attempts_per_step * args.steps / (t_dev * 1e9)
+
+    # e2e through the C ABI with host buffers (pinned)
+    h_w = torch.zeros(N + 1, dtype=torch.float64).pin_memory()
+    h_hist = torch.zeros(N + 1, dtype=torch.int64).pin_memory()
+    w_np = h_w.numpy()
+    hist_np = h_hist.numpy().view(np.uint64)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        eng.set_weights(w_np)
+        eng.sweep(k, 100, 1000, N, N)
+        eng.update_weights(m.UPDATE_TRIVIAL, wait=True)
+        eng.get_weights(out=w_np)
+        eng.histogram(out=hist_np)
+        k += 1
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = ws * attempts_per_step * args.steps / (t_e2e * 1e9)
+
+    out = None
+    if rank == 0:
+        peaks = measured_peaks()
+        hbm_peak = peaks["hbm_gbs"] if peaks else 6800.0
+        sweep_avg = t_sweep / args.steps
+        att_rate = attempts_per_step / sweep_avg
+        prof = profile_traffic()
+        philox_peak = m.philox_peak(local, 7)
+        out = {
+            "metric": METRIC, "value": value, "unit": "attempts/ns", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
+            "data": "synthetic (reference initial spins, weights start at zero and follow the trivial update)",
+            "config": {"workload": "weight-estimation iteration, L=%d (N=%d), %d chains, therm=N + nup=N attempts "
+                                   "per chain, FP64 trivial update" % (L, N, chains),
+                       "L": L, "chains_per_gpu": chains, "attempts_per_step_per_gpu": attempts_per_step,
+                       "l2": "flushed before every timed step (256 MiB write, outside the events)",
+                       "parallelism": "dp%d (independent chain shards, reference device = rank)" % ws,
+                       "chains_per_block": eng.info.chains_per_block, "blocks": eng.info.blocks,
+                       "smem_bytes": eng.info.smem_bytes},
+            "e2e": {"value": e2e, "unit": "attempts/ns", "h2d_bytes_per_step": 8 * (N + 1),
+                    "d2h_bytes_per_step": 16 * (N + 1) + 48,
+                    "path": "muca_set_weights -> muca_sweep -> muca_update_weights -> muca_get_weights/histogram"},
+            "roofline": {"bound": "hbm", "achieved": ALG_BYTES_PER_ATTEMPT * att_rate / 1e9, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": ALG_BYTES_PER_ATTEMPT * att_rate / 1e9 / hbm_peak,
+                         "traffic": prof.get("dram_bytes_per_launch") if prof else None,
+                         "peak_source": "measured" if peaks else "fallback",
+                         "note": "lattice resident in shared memory; HBM is not the bound (see roofline_int)"},
+            "roofline_int": {"bound": "int", "achieved": PHILOX_BLOCKS_PER_ATTEMPT * att_rate / 1e9,
+                             "peak": philox_peak / 1e9, "unit": "G Philox4x32-7 blocks/s",
+                             "frac": PHILOX_BLOCKS_PER_ATTEMPT * att_rate / philox_peak,
+                             "peak_source": "measured (muca_philox_peak on this GPU)"},
+            "sweep_ms": 1e3 * sweep_avg, "gpu_launches": 2 * args.steps,
+            "clocks": clk, "wall_s_timed_region": t_wall,
+        }
+    eng.close()
+    if rank == 0 and ws == 1 and not args.no_ref_gpu:
+        out["ref_gpu_kernel"] = ref_gpu_kernel_rate(L, chains)
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        v, sample = cpu_oracle_rate(L, chains, nthreads)
+        out["cpu_baseline"] = {"value": v, "unit": "attempts/ns", "cores": nthreads, "kind": "port",
+                               "sample": sample}
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def ref_gpu_kernel_rate(L, chains):
+    """The reference weight kernel (muca_delta_multigpu.cu:737-829, compiled
+    unchanged for sm_103a) on the same step, at the config's chain count and
+    at the reference's own default (maxThreadsPerSM * SMs)."""
+    try:
+        import numpy as np
+        from oracle import orc
+        orc.build(refgpu=True)
+        if orc.refgpu() is None:
+            return {"unavailable": "reference cubins not present"}
+        import muca_gb300 as m
+        N = L * L
+        res = {"unit": "attempts/ns", "step": "therm=N + nup=N attempts per chain, one launch"}
+        for label, nw in (("config_chains", chains), ("reference_default_chains", m.default_chains(0))):
+            nw = nw // 256 * 256
+            lat = orc.init_lattice(L, nw, orc.scheme_weight(0, 0))
+            ej, ed, _ = orc.energies(L, lat)
+            w32 = np.zeros(N + 1, np.float32)
+            orc.refgpu_weight(L, lat, w32, ej, ed, 0, 100, N, 0)  # warm-up (load, first launch)
+            _, _, _, _, ms = orc.refgpu_weight(L, lat, w32, ej, ed, 1, 100, N, N)
+            res[label] = {"chains": nw, "value": nw * 2 * N / (ms * 1e6), "ms": ms}
+        return res
+    except Exception as ex:  # report, never fail the bench on the extra line
+        return {"unavailable": str(ex)[:200]}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return reference_arm(args, ws, rank)
+    return ours_arm(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

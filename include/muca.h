@@ -1,0 +1,215 @@
+/*
+ * muca.h -- C ABI of the GB300 multicanonical (MUCA) engine for the 2D
+ * Blume-Capel model.
+ *
+ * The reference (null2p/MUCA) has no library interface: its boundary is the
+ * command line and files of two CUDA programs, multigpu_weight
+ * (muca_delta_multigpu.cu) and produce_gpu (produce2_multigpu.cu).  This ABI
+ * is the layer underneath the drop-in executables of this project (which keep
+ * that command line and those files); each entry point names the reference
+ * code it replaces.  Plain pointers and sizes only: host buffers are owned by
+ * the caller, device buffers by the context.
+ *
+ * Conventions
+ *  - Every call returns a muca_status; muca_last_error() gives the text.
+ *  - A context serves one host thread and one CUDA stream.  It is not
+ *    thread-safe; separate contexts may be driven from separate threads.
+ *  - Lattices cross the ABI as int8 [chain][site], site = row*L + col, spins
+ *    in {-1, 0, +1}.  Chain c is the reference's WORKER c of emulated device
+ *    c / nchains (the reference's starting_gpu..last_gpu range becomes
+ *    `ndev` emulated devices on one GPU, each with its own seeds).
+ *  - The multicanonical variable is E_Delta = sum_i s_i^2 in [0, N], N = L*L
+ *    (muca_delta_multigpu.cu:195,810,823); weights and the weight-run
+ *    histogram have N+1 entries.  The production histogram is over
+ *    (E_Delta, M) packed at (M + E_Delta^2 + 2 E_Delta)/2, (N+1)(N+2)/2
+ *    entries (produce2_multigpu.cu:489).
+ *  - beta = 2 (T = 0.5) is fixed in the Metropolis step, as in the
+ *    reference (muca_delta_multigpu.cu:810).
+ */
+#ifndef MUCA_H
+#define MUCA_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MUCA_ABI_VERSION 1
+
+typedef struct muca_ctx muca_ctx;
+
+typedef enum muca_status {
+    MUCA_OK = 0,
+    MUCA_ERR_BAD_ARG = 1,       /* invalid argument (size, L, pointer, lattice value) */
+    MUCA_ERR_CUDA = 2,          /* a CUDA call failed */
+    MUCA_ERR_TIMEOUT = 3,       /* a bounded device loop gave up */
+    MUCA_ERR_NOT_CONVERGED = 4, /* weight run hit max_iter */
+    MUCA_ERR_IO = 5,            /* file read/write failed or malformed file */
+    MUCA_ERR_STATE = 6          /* call not valid in the current context state */
+} muca_status;
+
+typedef enum muca_mode {
+    MUCA_MODE_WEIGHT = 0,  /* FP32 weight shadow, 1D histogram of E_Delta (multigpu_weight) */
+    MUCA_MODE_PRODUCE = 1  /* FP64 weights, M tracked, 2D (E_Delta, M) histogram (produce_gpu) */
+} muca_mode;
+
+typedef enum muca_init_scheme {
+    MUCA_INIT_WEIGHT = 0,   /* muca_delta_multigpu.cu:340-351: key {10W+2*jack, 0xdecafbad},
+                               ctr {2*dev, 100, 0xBADCAB1E, 0xBADC0DED}, ++ctr[0] per 4 sites */
+    MUCA_INIT_PRODUCE = 1,  /* produce2_multigpu.cu:126-138: key {10W, 0xdecafbad},
+                               ctr {1000*dev, 100, 0, 0xBADCAFE3}, ++ctr[2] per 4 sites */
+    MUCA_INIT_BASELINE = 2, /* extension: Philox4x32-10, key {2024, jack}, ctr {chain, group, 0, 0} */
+    MUCA_INIT_ORDERED = 3   /* extension for rand_config=0: every spin +1 */
+} muca_init_scheme;
+
+typedef enum muca_update_rule {
+    MUCA_UPDATE_TRIVIAL = 0,     /* muca_delta_multigpu.cu:466-476: lnW -= ln H for H>1; lnW -= lnW[0] */
+    MUCA_UPDATE_TRIVIAL_CPU = 1, /* muca_mag.cpp:178-183: H>0 variant, normalise bins with H>0 only */
+    MUCA_UPDATE_RECURSION = 2    /* muca_delta_multigpu.cu:833-859 weight_recursion, then lnW -= lnW[0] */
+} muca_update_rule;
+
+typedef struct muca_params {
+    uint32_t L;        /* lattice side, 2..128 */
+    uint32_t nchains;  /* chains per emulated device (reference NUM_WORKERS);
+                          0 = reference formula maxThreadsPerSM * SMs (muca_delta_multigpu.cu:100-106) */
+    uint32_t ndev;     /* emulated devices (reference last_gpu-starting_gpu+1); 0 means 1 */
+    int32_t device;    /* CUDA device ordinal */
+    uint32_t rounds;   /* Philox4x32 rounds: 7 (reference, muca_delta_multigpu.cu:21) or 10; 0 means 7 */
+    uint32_t mode;     /* muca_mode */
+    void *stream;      /* cudaStream_t to launch on; NULL = the context creates one */
+    uint32_t dev_offset; /* index of the first emulated device (a process that runs
+                            reference devices k..k+ndev-1 sets k; seeds and init
+                            counters follow the device index) */
+} muca_params;
+
+typedef struct muca_info {
+    uint32_t L, N, nchains_total, chains_per_block, blocks, lattice_in_smem, hist_in_smem;
+    uint32_t smem_bytes, sms, weights_in_smem;
+    uint64_t device_bytes;
+} muca_info;
+
+/* Histogram summary (muca_delta_multigpu.cu:431-447 and the min/mean test of
+ * the flatness criterion): range of bins with H>1 (hist_range :573-596),
+ * Kullback-Leibler divergence against uniform over visited bins (:598-618). */
+typedef struct muca_hist_stats {
+    int32_t start, end;       /* first/last bin with H > 1; 0,0 if none */
+    uint32_t width;           /* end - start */
+    uint32_t visited;         /* bins with H > 0 */
+    uint64_t events;          /* sum of H */
+    uint64_t min_count;       /* min over all N+1 bins */
+    double d_kl;              /* Kullback-Leibler divergence */
+    double min_over_mean;     /* min H / mean H over all N+1 bins */
+} muca_hist_stats;
+
+/* Options of a full weight-estimation run (muca_delta_multigpu.cu:329-477). */
+typedef struct muca_run_opts {
+    uint32_t jack;          /* jack index mm (init key 10W + 2*mm) */
+    uint32_t starting_M;    /* initial NUPDATES (argv[5]) */
+    uint32_t therm;         /* thermalisation attempts per chain per iteration; 0 = N (therm_coeff*N) */
+    uint32_t rule;          /* muca_update_rule */
+    uint32_t hold_until_full; /* 1: no update before width==N (muca_mag.cpp:170-177 intent);
+                                 0: update every iteration (what the GPU program does, :466) */
+    uint32_t flat_minmean;  /* 0: stop at width==N && D_KL<1e-4 (:447); 1: stop at min/mean >= 0.5 */
+    uint32_t max_iter;      /* iteration cap (0 = 1000000) */
+    uint32_t init_scheme;   /* muca_init_scheme for the chains; MUCA_INIT_WEIGHT for parity */
+    uint32_t reinit_chains; /* 1: initialise chains at the start (the reference does, :340-354) */
+    uint32_t nup_schedule;  /* 0: reference ((NUP+1)*1.01 once width==N, :379-382); 1: doubling */
+    double min_over_mean;   /* threshold for flat_minmean (0 = 0.5) */
+    double d_kl_max;        /* threshold of the D_KL test (0 = 1e-4) */
+} muca_run_opts;
+
+typedef struct muca_iter_record {
+    uint32_t k, width_temp, width, nupdates;
+    uint64_t total_run;
+    double d_kl, min_over_mean, kernel_ms, memcpy_ms;
+} muca_iter_record;
+
+typedef struct muca_run_result {
+    uint32_t iterations, converged, width_reached_iter;
+    uint64_t total_run, nwidth_step;
+    double total_kernel_s, total_mem_s, nwidth_time_s, wall_s;
+} muca_run_result;
+
+/* Observables of one reweighted production histogram
+ * (produce2_multigpu.cu:498-518, plus the Binder cumulant as an extension). */
+typedef struct muca_observables {
+    double m_abs;   /* <|M|> (not divided by N, as in the reference) */
+    double chi;     /* beta (<M^2> - <|M|>^2) / N */
+    double u4;      /* 1 - <M^4> / (3 <M^2>^2) */
+    double sum, m1, m2, m4;
+} muca_observables;
+
+/* ---------------------------------------------------------------------- */
+/* Context.  Replaces the per-device set-up of main() in
+ * muca_delta_multigpu.cu:93-205 / produce2_multigpu.cu:103-275. */
+muca_status muca_create(const muca_params *params, muca_ctx **out);
+muca_status muca_destroy(muca_ctx *ctx);
+const char *muca_last_error(const muca_ctx *ctx);
+muca_status muca_get_info(const muca_ctx *ctx, muca_info *out);
+/* reference NUM_WORKERS formula of the device (muca_delta_multigpu.cu:100-106) */
+muca_status muca_default_chains(int32_t device, uint32_t *out);
+
+/* Chains.  Replaces the host lattice init (muca_delta_multigpu.cu:340-354,
+ * produce2_multigpu.cu:126-140) and computeEnergies/computeDeltaE/computeM
+ * (muca_delta_multigpu.cu:69-83, produce2_multigpu.cu:66-89), on the device. */
+muca_status muca_init_chains(muca_ctx *ctx, uint32_t scheme, uint32_t jack);
+muca_status muca_set_lattice(muca_ctx *ctx, const int8_t *lat, size_t n);
+muca_status muca_get_lattice(muca_ctx *ctx, int8_t *lat, size_t n);
+muca_status muca_get_chain_state(muca_ctx *ctx, int32_t *e_j, int32_t *e_delta, int32_t *mag, size_t n);
+
+/* Weights.  Replaces the H2D copy of the FP32 weight (muca_delta_multigpu.cu:384-387)
+ * and of the FP64 weight (produce2_multigpu.cu:262). */
+muca_status muca_set_weights(muca_ctx *ctx, const double *lnw, size_t n);
+muca_status muca_get_weights(muca_ctx *ctx, double *lnw, size_t n);
+
+/* One sweep launch: `therm` attempts per chain, then `nup` attempts per
+ * chain with a histogram entry after each.  Replaces one launch of kernel
+ * mcs (muca_delta_multigpu.cu:393 / produce2_multigpu.cu:301,311).  The
+ * histogram is cleared first (the reference clears it inside the kernel,
+ * racily, :746-749).  seed of emulated device d = seed_base + seed_dev_mul*d
+ * (the reference passes SEED+1000*l, SEED+1000*GPU+l, SEED+2000*GPU). */
+muca_status muca_sweep(muca_ctx *ctx, uint32_t iter, uint32_t seed_base, uint32_t seed_dev_mul,
+                       uint64_t therm, uint64_t nup);
+/* Same, but accumulate into the histogram instead of clearing it. */
+muca_status muca_sweep_accumulate(muca_ctx *ctx, uint32_t iter, uint32_t seed_base, uint32_t seed_dev_mul,
+                                  uint64_t therm, uint64_t nup);
+muca_status muca_clear_histogram(muca_ctx *ctx);
+/* n = N+1 (weight mode) or (N+1)(N+2)/2 (production mode); u64 counts.
+ * The reference copies the histogram to the host after every launch
+ * (muca_delta_multigpu.cu:404-429, produce2_multigpu.cu:313-316); here it
+ * stays on the device and is read only on request.  set_histogram restores
+ * a saved histogram (checkpoint/resume, tests). */
+muca_status muca_get_histogram(muca_ctx *ctx, uint64_t *h, size_t n);
+muca_status muca_set_histogram(muca_ctx *ctx, const uint64_t *h, size_t n);
+
+/* Weight update on the device in FP64.  Replaces the host update
+ * muca_delta_multigpu.cu:466-476 (and :833-859 for the recursion); the
+ * FP32 shadow used by the next sweep is refreshed.  `stats` (optional)
+ * receives the summary of the histogram the update used; with stats == NULL
+ * the update is only enqueued on the context's stream (no host wait). */
+muca_status muca_histogram_stats(muca_ctx *ctx, muca_hist_stats *stats);
+muca_status muca_update_weights(muca_ctx *ctx, uint32_t rule, muca_hist_stats *stats);
+
+/* Full weight-estimation run of one jack (muca_delta_multigpu.cu:329-477).
+ * recs (optional, capacity cap) receives one record per iteration. */
+muca_status muca_weight_run(muca_ctx *ctx, const muca_run_opts *opts, muca_run_result *res,
+                            muca_iter_record *recs, size_t cap);
+
+/* Production.  Shift lnW (produce2_multigpu.cu:391-400), form
+ * boltz_j = exp(-beta*delta*j - lnW_j) (:297) and reweight the current 2D
+ * histogram into observables (:498-518), all on the device in FP64. */
+muca_status muca_weight_shift(muca_ctx *ctx, double beta, double delta);
+muca_status muca_compute_observables(muca_ctx *ctx, double beta, double delta, muca_observables *out);
+/* Leave-one-out jackknife (muca_delta_multigpu.cu:620-635) on the device. */
+muca_status muca_jackknife(muca_ctx *ctx, const double *x, uint32_t n, double *avg, double *err);
+
+/* Measurement (no reference counterpart): Philox4x32-R blocks per second
+ * generated by a full-occupancy kernel in the form the sweeps use, the
+ * integer-pipe ceiling against which the sweep kernels are reported. */
+muca_status muca_philox_peak(int32_t device, uint32_t rounds, double *blocks_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

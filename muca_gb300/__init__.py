@@ -1,0 +1,281 @@
+"""muca_gb300 -- GB300-native multicanonical (MUCA) engine for the 2D
+Blume-Capel model.
+
+This module is a thin ctypes binding of the C ABI in include/muca.h, which is
+implemented by hand-written sm_103a CUDA kernels in muca_gb300/csrc and built
+into muca_gb300/_build/libmuca.so.  There is no CPU fallback: if the library
+is missing or no GPU is present the calls raise.
+
+The drop-in replacements for the reference programs multigpu_weight and
+produce_gpu are the executables muca_gb300/_build/{multigpu_weight,produce_gpu}
+(same positional command line, same output files).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmuca.so")
+
+MODE_WEIGHT, MODE_PRODUCE = 0, 1
+INIT_WEIGHT, INIT_PRODUCE, INIT_BASELINE, INIT_ORDERED = 0, 1, 2, 3
+UPDATE_TRIVIAL, UPDATE_TRIVIAL_CPU, UPDATE_RECURSION = 0, 1, 2
+STATUS = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "TIMEOUT", 4: "NOT_CONVERGED", 5: "IO", 6: "STATE"}
+
+# Every symbol include/muca.h declares (the C-ABI surface).
+EXPORTS = [
+    "muca_create", "muca_destroy", "muca_last_error", "muca_get_info", "muca_default_chains",
+    "muca_init_chains", "muca_set_lattice", "muca_get_lattice", "muca_get_chain_state",
+    "muca_set_weights", "muca_get_weights", "muca_sweep", "muca_sweep_accumulate",
+    "muca_clear_histogram", "muca_get_histogram", "muca_set_histogram", "muca_histogram_stats", "muca_update_weights",
+    "muca_weight_run", "muca_weight_shift", "muca_compute_observables", "muca_jackknife",
+    "muca_philox_peak",
+]
+
+
+class MucaError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class Params(C.Structure):
+    _fields_ = [("L", C.c_uint32), ("nchains", C.c_uint32), ("ndev", C.c_uint32), ("device", C.c_int32),
+                ("rounds", C.c_uint32), ("mode", C.c_uint32), ("stream", C.c_void_p), ("dev_offset", C.c_uint32)]
+
+
+class Info(C.Structure):
+    _fields_ = [("L", C.c_uint32), ("N", C.c_uint32), ("nchains_total", C.c_uint32),
+                ("chains_per_block", C.c_uint32), ("blocks", C.c_uint32), ("lattice_in_smem", C.c_uint32),
+                ("hist_in_smem", C.c_uint32), ("smem_bytes", C.c_uint32), ("sms", C.c_uint32),
+                ("weights_in_smem", C.c_uint32), ("device_bytes", C.c_uint64)]
+
+
+class HistStats(C.Structure):
+    _fields_ = [("start", C.c_int32), ("end", C.c_int32), ("width", C.c_uint32), ("visited", C.c_uint32),
+                ("events", C.c_uint64), ("min_count", C.c_uint64), ("d_kl", C.c_double),
+                ("min_over_mean", C.c_double)]
+
+
+class RunOpts(C.Structure):
+    _fields_ = [("jack", C.c_uint32), ("starting_M", C.c_uint32), ("therm", C.c_uint32), ("rule", C.c_uint32),
+                ("hold_until_full", C.c_uint32), ("flat_minmean", C.c_uint32), ("max_iter", C.c_uint32),
+                ("init_scheme", C.c_uint32), ("reinit_chains", C.c_uint32), ("nup_schedule", C.c_uint32),
+                ("min_over_mean", C.c_double), ("d_kl_max", C.c_double)]
+
+
+class IterRecord(C.Structure):
+    _fields_ = [("k", C.c_uint32), ("width_temp", C.c_uint32), ("width", C.c_uint32), ("nupdates", C.c_uint32),
+                ("total_run", C.c_uint64), ("d_kl", C.c_double), ("min_over_mean", C.c_double),
+                ("kernel_ms", C.c_double), ("memcpy_ms", C.c_double)]
+
+
+class RunResult(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("converged", C.c_uint32), ("width_reached_iter", C.c_uint32),
+                ("total_run", C.c_uint64), ("nwidth_step", C.c_uint64), ("total_kernel_s", C.c_double),
+                ("total_mem_s", C.c_double), ("nwidth_time_s", C.c_double), ("wall_s", C.c_double)]
+
+
+class Observables(C.Structure):
+    _fields_ = [("m_abs", C.c_double), ("chi", C.c_double), ("u4", C.c_double), ("sum", C.c_double),
+                ("m1", C.c_double), ("m2", C.c_double), ("m4", C.c_double)]
+
+
+_LIB = None
+
+
+def lib():
+    """Load libmuca.so (raises if it was not built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("muca_gb300: %s is missing; run `python -c 'import __graft_entry__ as g; g.build()'`"
+                          % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    i8 = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
+    i32 = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    u64 = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+    f64 = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    L.muca_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
+    L.muca_destroy.argtypes = [vp]
+    L.muca_last_error.argtypes = [vp]
+    L.muca_last_error.restype = C.c_char_p
+    L.muca_get_info.argtypes = [vp, C.POINTER(Info)]
+    L.muca_default_chains.argtypes = [C.c_int32, C.POINTER(C.c_uint32)]
+    L.muca_init_chains.argtypes = [vp, C.c_uint32, C.c_uint32]
+    L.muca_set_lattice.argtypes = [vp, i8, C.c_size_t]
+    L.muca_get_lattice.argtypes = [vp, i8, C.c_size_t]
+    L.muca_get_chain_state.argtypes = [vp, i32, i32, i32, C.c_size_t]
+    L.muca_set_weights.argtypes = [vp, f64, C.c_size_t]
+    L.muca_get_weights.argtypes = [vp, f64, C.c_size_t]
+    L.muca_sweep.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint64]
+    L.muca_sweep_accumulate.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint64]
+    L.muca_clear_histogram.argtypes = [vp]
+    L.muca_get_histogram.argtypes = [vp, u64, C.c_size_t]
+    L.muca_set_histogram.argtypes = [vp, u64, C.c_size_t]
+    L.muca_histogram_stats.argtypes = [vp, C.POINTER(HistStats)]
+    L.muca_update_weights.argtypes = [vp, C.c_uint32, C.POINTER(HistStats)]
+    L.muca_weight_run.argtypes = [vp, C.POINTER(RunOpts), C.POINTER(RunResult), C.POINTER(IterRecord), C.c_size_t]
+    L.muca_weight_shift.argtypes = [vp, C.c_double, C.c_double]
+    L.muca_compute_observables.argtypes = [vp, C.c_double, C.c_double, C.POINTER(Observables)]
+    L.muca_jackknife.argtypes = [vp, f64, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.muca_philox_peak.argtypes = [C.c_int32, C.c_uint32, C.POINTER(C.c_double)]
+    _LIB = L
+    return L
+
+
+def philox_peak(device: int = 0, rounds: int = 7) -> float:
+    """Measured Philox4x32-R blocks per second on this GPU (integer-pipe ceiling)."""
+    out = C.c_double()
+    st = lib().muca_philox_peak(device, rounds, C.byref(out))
+    if st:
+        raise MucaError(st, lib().muca_last_error(None).decode())
+    return out.value
+
+
+def default_chains(device: int = 0) -> int:
+    out = C.c_uint32()
+    st = lib().muca_default_chains(device, C.byref(out))
+    if st:
+        raise MucaError(st, lib().muca_last_error(None).decode())
+    return out.value
+
+
+class Engine:
+    """One simulation context (all chains of one lattice size) on one GPU."""
+
+    def __init__(self, L, nchains=0, ndev=1, mode=MODE_WEIGHT, rounds=7, device=0, stream=None, dev_offset=0):
+        self._lib = lib()
+        p = Params(L=L, nchains=nchains, ndev=ndev, device=device, rounds=rounds, mode=mode,
+                   stream=C.c_void_p(stream) if stream else None, dev_offset=dev_offset)
+        h = C.c_void_p()
+        st = self._lib.muca_create(C.byref(p), C.byref(h))
+        if st:
+            raise MucaError(st, self._lib.muca_last_error(None).decode())
+        self._h = h
+        self.L, self.N, self.mode = L, L * L, mode
+        self.info = self._info()
+        self.nchains = self.info.nchains_total
+
+    # -- plumbing --------------------------------------------------------
+    def _ck(self, st):
+        if st:
+            raise MucaError(st, self._lib.muca_last_error(self._h).decode())
+
+    def _info(self):
+        i = Info()
+        self._ck(self._lib.muca_get_info(self._h, C.byref(i)))
+        return i
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.muca_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- chains / weights --------------------------------------------------
+    def init_chains(self, scheme=INIT_WEIGHT, jack=0):
+        self._ck(self._lib.muca_init_chains(self._h, scheme, jack))
+
+    def set_lattice(self, lat):
+        a = np.ascontiguousarray(lat, np.int8).reshape(-1)
+        self._ck(self._lib.muca_set_lattice(self._h, a, a.size))
+
+    def get_lattice(self):
+        a = np.zeros(self.nchains * self.N, np.int8)
+        self._ck(self._lib.muca_get_lattice(self._h, a, a.size))
+        return a.reshape(self.nchains, self.N)
+
+    def chain_state(self):
+        ej = np.zeros(self.nchains, np.int32)
+        ed = np.zeros(self.nchains, np.int32)
+        mg = np.zeros(self.nchains, np.int32)
+        self._ck(self._lib.muca_get_chain_state(self._h, ej, ed, mg, self.nchains))
+        return ej, ed, mg
+
+    def set_weights(self, lnw):
+        a = np.ascontiguousarray(lnw, np.float64)
+        self._ck(self._lib.muca_set_weights(self._h, a, a.size))
+
+    def get_weights(self, out=None):
+        a = np.zeros(self.N + 1) if out is None else out
+        self._ck(self._lib.muca_get_weights(self._h, a, a.size))
+        return a
+
+    # -- sweeps ----------------------------------------------------------
+    def sweep(self, iter_, seed_base, seed_dev_mul, therm, nup, accumulate=False):
+        f = self._lib.muca_sweep_accumulate if accumulate else self._lib.muca_sweep
+        self._ck(f(self._h, iter_, seed_base, seed_dev_mul, therm, nup))
+
+    def clear_histogram(self):
+        self._ck(self._lib.muca_clear_histogram(self._h))
+
+    def histogram(self, out=None):
+        n = self.N + 1 if self.mode == MODE_WEIGHT else (self.N + 1) * (self.N + 2) // 2
+        h = np.zeros(n, np.uint64) if out is None else out
+        self._ck(self._lib.muca_get_histogram(self._h, h, n))
+        return h
+
+    def set_histogram(self, h):
+        a = np.ascontiguousarray(h, np.uint64)
+        self._ck(self._lib.muca_set_histogram(self._h, a, a.size))
+
+    def hist_stats(self):
+        s = HistStats()
+        self._ck(self._lib.muca_histogram_stats(self._h, C.byref(s)))
+        return s
+
+    def update_weights(self, rule=UPDATE_TRIVIAL, wait=True):
+        """FP64 weight update on the device; wait=False only enqueues it."""
+        if not wait:
+            self._ck(self._lib.muca_update_weights(self._h, rule, None))
+            return None
+        s = HistStats()
+        self._ck(self._lib.muca_update_weights(self._h, rule, C.byref(s)))
+        return s
+
+    def weight_run(self, starting_M=1, jack=0, rule=UPDATE_TRIVIAL, hold_until_full=0, flat_minmean=0,
+                   max_iter=0, therm=0, init_scheme=INIT_WEIGHT, reinit_chains=1, nup_schedule=0,
+                   min_over_mean=0.0, d_kl_max=0.0, records=1000, raise_on_not_converged=False):
+        o = RunOpts(jack=jack, starting_M=starting_M, therm=therm, rule=rule, hold_until_full=hold_until_full,
+                    flat_minmean=flat_minmean, max_iter=max_iter, init_scheme=init_scheme,
+                    reinit_chains=reinit_chains, nup_schedule=nup_schedule, min_over_mean=min_over_mean,
+                    d_kl_max=d_kl_max)
+        res = RunResult()
+        recs = (IterRecord * max(records, 1))()
+        st = self._lib.muca_weight_run(self._h, C.byref(o), C.byref(res), recs, records)
+        if st and (st != 4 or raise_on_not_converged):
+            self._ck(st)
+        n = min(res.iterations, records)
+        return res, [recs[i] for i in range(n)]
+
+    # -- production --------------------------------------------------------
+    def weight_shift(self, beta, delta):
+        self._ck(self._lib.muca_weight_shift(self._h, beta, delta))
+
+    def observables(self, beta, delta):
+        o = Observables()
+        self._ck(self._lib.muca_compute_observables(self._h, beta, delta, C.byref(o)))
+        return o
+
+    def jackknife(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        a, e = C.c_double(), C.c_double()
+        self._ck(self._lib.muca_jackknife(self._h, x, x.size, C.byref(a), C.byref(e)))
+        return a.value, e.value

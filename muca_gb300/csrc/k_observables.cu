@@ -1,0 +1,157 @@
+// k_observables.cu -- production reweighting on the device, FP64.
+//
+// Replaces the host code of the reference production program that runs per
+// Delta point: weight_shift (produce2_multigpu.cu:391-400), the Boltzmann
+// factors boltz_j = exp(-beta*delta*j - lnW_j) (:297), the reweighting sums
+// over the triangular (E_Delta, M) histogram (observables, :498-518; the
+// reference sums in x87 long double on the host) and the jackknife
+// (:520-535).  The triangle's row i (E_Delta = i) holds the i+1 bins
+// m = -i, -i+2, ..., i at (i^2 + 2i + m)/2 = i(i+1)/2 + (m+i)/2.
+//
+// The sums stream the u64 histogram once (HBM bound at 8 B per bin); empty
+// bins cost no FP64 work.  Each term is formed as the reference forms it:
+// (double)(|m| H) * boltz_i, (double)(m^2 H) * boltz_i; partial sums are
+// combined per warp, per block and then in a fixed-order second pass, so the
+// result is deterministic and agrees with the long-double host sum to ~1e-15.
+#include "muca_device.cuh"
+#include "muca_internal.h"
+
+namespace muca {
+
+constexpr int kObsThreads = 256;
+constexpr int kObsBlocks = 152 * 4;  // a multiple of the SM count (152 on GB300)
+
+__global__ void k_weight_shift(double *lnw, uint32_t N, double beta, double delta)
+{
+    __shared__ double sh[32];
+    const double bd = __dmul_rn(beta, delta);
+    double mx = -1.0 / 0.0;
+    for (uint32_t i = threadIdx.x; i <= N; i += blockDim.x) {
+        const double v = __dsub_rn(-lnw[i], __dmul_rn(bd, (double)i));
+        mx = v > mx ? v : mx;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) { const double t = __shfl_xor_sync(0xffffffffu, mx, o); mx = t > mx ? t : mx; }
+    if (lane == 0) sh[wid] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = sh[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = sh[w] > m ? sh[w] : m;
+        sh[0] = m;
+    }
+    __syncthreads();
+    const double m = sh[0];
+    for (uint32_t i = threadIdx.x; i <= N; i += blockDim.x) lnw[i] = __dadd_rn(lnw[i], m);
+}
+
+// Row i of the first bin b: largest i with i(i+1)/2 <= b.
+__device__ __forceinline__ uint32_t row_of(unsigned long long b)
+{
+    uint32_t i = (uint32_t)((sqrt(8.0 * (double)b + 1.0) - 1.0) * 0.5);
+    while ((unsigned long long)i * (i + 1) / 2 > b) --i;
+    while ((unsigned long long)(i + 1) * (i + 2) / 2 <= b) ++i;
+    return i;
+}
+
+__global__ void __launch_bounds__(kObsThreads) k_observables(const unsigned long long *__restrict__ hist,
+                                                             const double *__restrict__ lnw, uint32_t N,
+                                                             double beta, double delta,
+                                                             double *__restrict__ partials)
+{
+    const unsigned long long nb = (unsigned long long)(N + 1) * (N + 2) / 2;
+    const double nbd = __dmul_rn(-beta, delta);
+    double s0 = 0, s1 = 0, s2 = 0, s4 = 0;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    unsigned long long b = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (b < nb) {
+        uint32_t i = row_of(b);
+        unsigned long long row0 = (unsigned long long)i * (i + 1) / 2;
+        double bz = exp(__dsub_rn(__dmul_rn(nbd, (double)i), lnw[i]));
+        for (; b < nb; b += stride) {
+            while (b >= row0 + i + 1) {
+                row0 += i + 1;
+                ++i;
+                bz = -1.0;  // recomputed below when a nonzero bin needs it
+            }
+            const unsigned long long H = __ldcs(hist + b);
+            if (H == 0) continue;
+            if (bz < 0.0) bz = exp(__dsub_rn(__dmul_rn(nbd, (double)i), lnw[i]));
+            const int m = 2 * (int)(b - row0) - (int)i;
+            const unsigned long long am = (unsigned long long)(m < 0 ? -m : m);
+            const double t0 = __dmul_rn((double)H, bz);
+            const double t2 = __dmul_rn((double)(am * am * H), bz);
+            s0 = __dadd_rn(s0, t0);
+            s1 = __dadd_rn(s1, __dmul_rn((double)(am * H), bz));
+            s2 = __dadd_rn(s2, t2);
+            s4 = __dadd_rn(s4, __dmul_rn(t2, (double)(am * am)));
+        }
+    }
+    __shared__ double sh[4][kObsThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        s4 += __shfl_xor_sync(0xffffffffu, s4, o);
+    }
+    if (lane == 0) { sh[0][wid] = s0; sh[1][wid] = s1; sh[2][wid] = s2; sh[3][wid] = s4; }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0;
+        for (int w = 0; w < kObsThreads / 32; ++w) t += sh[threadIdx.x][w];
+        partials[(size_t)blockIdx.x * 4 + threadIdx.x] = t;
+    }
+}
+
+__global__ void k_observables_final(const double *partials, int nblocks, double *out)
+{
+    if (threadIdx.x < 4) {
+        double t = 0;
+        for (int b = 0; b < nblocks; ++b) t += partials[(size_t)b * 4 + threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+}
+
+// jakknife (muca_delta_multigpu.cu:620-635), one thread, same order.
+__global__ void k_jackknife(const double *x, uint32_t J, double *out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double avg = 0;
+    for (uint32_t i = 0; i < J; i++) avg += x[i];
+    const double total = avg;
+    avg = avg / (double)J;
+    double dev = 0;
+    for (uint32_t i = 0; i < J; i++) {
+        const double mi = (total - x[i]) / (double)(J - 1);
+        dev += (avg - mi) * (avg - mi);
+    }
+    dev = (double)(J - 1) * dev / (double)J;
+    out[0] = avg;
+    out[1] = sqrt(dev);
+}
+
+cudaError_t launch_weight_shift(double *lnw, uint32_t N, double beta, double delta, cudaStream_t s)
+{
+    k_weight_shift<<<1, 1024, 0, s>>>(lnw, N, beta, delta);
+    return cudaGetLastError();
+}
+
+size_t observables_partials(uint32_t) { return (size_t)kObsBlocks * 4; }
+
+cudaError_t launch_observables(const unsigned long long *hist2d, const double *lnw, uint32_t N, double beta,
+                               double delta, double *partials, double *out, cudaStream_t s)
+{
+    k_observables<<<kObsBlocks, kObsThreads, 0, s>>>(hist2d, lnw, N, beta, delta, partials);
+    k_observables_final<<<1, 32, 0, s>>>(partials, kObsBlocks, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_jackknife(const double *x, uint32_t n, double *out2, cudaStream_t s)
+{
+    k_jackknife<<<1, 32, 0, s>>>(x, n, out2);
+    return cudaGetLastError();
+}
+
+}  // namespace muca

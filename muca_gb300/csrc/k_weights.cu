@@ -1,0 +1,255 @@
+// k_weights.cu -- histogram statistics and weight updates on the device, FP64.
+//
+// Replaces the host code that runs after every sweep of the reference weight
+// program (muca_delta_multigpu.cu:422-476): hist_range (:573-596), the
+// Kullback-Leibler divergence against a uniform distribution over visited
+// bins (:598-618), the trivial update lnW -= ln H for H > 1 followed by
+// lnW -= lnW[0] (:466-476), and weight_recursion (:833-859).  One block
+// serves one histogram of N+1 <= 16385 bins.  Element-wise steps use the
+// reference's operation order with explicitly rounded FP64 operations, so
+// the updated weights equal the host's up to the last-bit differences of the
+// device and host log(); the divergence is a tree sum and agrees to ~1e-15.
+#include "muca_device.cuh"
+#include "muca_internal.h"
+
+#include <cfloat>
+
+namespace muca {
+
+constexpr int kUpdThreads = 1024;
+
+template <typename T, typename Op>
+__device__ T block_reduce(T v, Op op, T *sh)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < nw ? sh[lane] : sh[0];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) sh[0] = v;
+    }
+    __syncthreads();
+    const T r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+struct MinI { __device__ int operator()(int a, int b) const { return a < b ? a : b; } };
+struct MaxI { __device__ int operator()(int a, int b) const { return a > b ? a : b; } };
+struct AddU { __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return a + b; } };
+struct MinU { __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return a < b ? a : b; } };
+struct AddD { __device__ double operator()(double a, double b) const { return a + b; } };
+
+// Statistics of hist[0..N], then (if the update is due) the weight update.
+// ctl == nullptr: standalone call, update iff rule >= 0.
+// ctl != nullptr: one iteration of a device-driven run (see RunCtl).
+__global__ void __launch_bounds__(kUpdThreads) k_weight_update(const unsigned long long *__restrict__ hist, uint32_t N,
+                                                                double *__restrict__ lnw, float *__restrict__ w32,
+                                                                double *__restrict__ p_acc, int rule,
+                                                                HistStatsDev *__restrict__ stats,
+                                                                RunCtl *__restrict__ ctl)
+{
+    extern __shared__ __align__(16) unsigned char dyn[];
+    __shared__ int shi[32];
+    __shared__ unsigned long long shu[32];
+    __shared__ double shd[32];
+    __shared__ int do_update;
+    const uint32_t tid = threadIdx.x, bs = blockDim.x;
+    if (ctl && ctl->st.stop) return;
+
+    // values needed before anything is written (normalisation constant)
+    const unsigned long long h0 = hist[0];
+    const double lnw0 = lnw[0];
+
+    int lo = (int)N + 1, hi = -1;
+    unsigned long long vis = 0, ev = 0, mn = ~0ull;
+    for (uint32_t i = tid; i <= N; i += bs) {
+        const unsigned long long h = hist[i];
+        if (h > 1) { lo = min(lo, (int)i); hi = max(hi, (int)i); }
+        if (h > 0) { ++vis; ev += h; }
+        mn = h < mn ? h : mn;
+    }
+    lo = block_reduce(lo, MinI(), shi);
+    hi = block_reduce(hi, MaxI(), shi);
+    vis = block_reduce(vis, AddU(), shu);
+    ev = block_reduce(ev, AddU(), shu);
+    mn = block_reduce(mn, MinU(), shu);
+    int start = lo, end = hi < 0 ? 0 : hi;
+    if (start > end) { start = 0; end = 0; }
+
+    // Kullback-Leibler divergence: sum over H>0 of P ln(P/Q), P = H/events, Q = 1/visited
+    const double num_event = (double)ev, Q = __ddiv_rn(1.0, (double)vis);
+    double kl = 0.0;
+    for (uint32_t i = tid; i <= N; i += bs) {
+        const unsigned long long h = hist[i];
+        if (h > 0) {
+            const double P = __ddiv_rn((double)h, num_event);
+            kl = __dadd_rn(kl, __dmul_rn(P, log(__ddiv_rn(P, Q))));
+        }
+    }
+    kl = block_reduce(kl, AddD(), shd);
+    const double mean = __ddiv_rn((double)ev, (double)(N + 1));
+    const double mom = mean > 0 ? __ddiv_rn((double)mn, mean) : 0.0;
+    if (tid == 0) {
+        if (stats) {
+            stats->start = start;
+            stats->end = end;
+            stats->width = (uint32_t)(end - start);
+            stats->visited = (uint32_t)vis;
+            stats->events = ev;
+            stats->min_count = mn;
+            stats->d_kl = kl;
+            stats->min_over_mean = mom;
+        }
+        int upd = rule >= 0;
+        if (ctl) {
+            // muca_delta_multigpu.cu:431-447,464-466
+            IterState &st = ctl->st;
+            const uint32_t wt = (uint32_t)(end - start);
+            st.width_temp = wt;
+            if (wt > st.width) st.width = wt;
+            if (st.width == N && !st.reach) { st.reach = 1; st.reach_k = st.k; st.nwidth_step = st.total_run; }
+            const bool conv = ctl->flat_minmean ? (mom >= ctl->mom_thr) : (st.width == N && kl < ctl->dkl_max);
+            if (st.k < ctl->rec_cap && ctl->recs) {
+                IterRecordDev &r = ctl->recs[st.k];
+                r.k = st.k; r.width_temp = wt; r.width = st.width; r.nupdates = st.nup;
+                r.total_run = st.total_run; r.d_kl = kl; r.min_over_mean = mom;
+            }
+            upd = !conv && (!ctl->hold || st.width == N);
+            if (conv) {
+                st.converged = 1;
+                st.stop = 1;
+            } else {
+                st.k += 1;
+                if (st.k >= ctl->max_iter) {
+                    st.stop = 1;
+                } else {
+                    if (st.width == N) {
+                        if (ctl->sched == 0) {
+                            unsigned nu = st.nup + 1u;           // :380-381
+                            st.nup = (unsigned)(nu * 1.01);
+                        } else {
+                            st.nup = st.nup * 2u;
+                        }
+                    }
+                    st.total_run += (unsigned long long)st.nup * ctl->nchains_total;
+                }
+            }
+        }
+        do_update = upd;
+    }
+    __syncthreads();
+    if (!do_update) return;
+
+    if (rule == 0 || rule == 1) {
+        // tmp = lnW[0] after the ln H subtraction (:469), computed from the
+        // values read before any write
+        const unsigned long long thr = rule == 0 ? 1ull : 0ull;
+        const double tmp = h0 > thr ? __dsub_rn(lnw0, log((double)h0)) : lnw0;
+        for (uint32_t i = tid; i <= N; i += bs) {
+            const unsigned long long h = hist[i];
+            double v = lnw[i];
+            if (h > thr) v = __dsub_rn(v, log((double)h));
+            if (rule == 0 || h > 0) v = __dsub_rn(v, tmp);
+            lnw[i] = v;
+            w32[i] = (float)v;
+        }
+        return;
+    }
+
+    // rule 2: weight_recursion (:848-858) then lnW -= lnW[0].
+    // (a) the increments dS_i of all connected pairs, in parallel;
+    double *ds = reinterpret_cast<double *>(dyn);
+    unsigned char *valid = dyn + sizeof(double) * (size_t)N;
+    for (uint32_t i = tid; i < N; i += bs) {
+        unsigned char ok = 0;
+        if ((int)i >= start && (int)i < end) {
+            const unsigned long long a = hist[i], b = hist[i + 1];
+            if ((a != 0) & (b != 0)) {
+                const double p = __ddiv_rn((double)(a * b), (double)(a + b));
+                const double k = __ddiv_rn(p, __dadd_rn(p, p_acc[i]));
+                const double lg = log(__ddiv_rn((double)a, (double)b));
+                ds[i] = __dadd_rn(__dadd_rn(-lnw[i], lnw[i + 1]), __dmul_rn(k, lg));
+                p_acc[i] = __dadd_rn(p_acc[i], p);
+                ok = 1;
+            }
+        }
+        valid[i] = ok;
+    }
+    __syncthreads();
+    // (b) the prefix lnW[i+1] = lnW[i] + dS_i, sequential as in the reference
+    //     (a pair with an empty bin leaves lnW[i+1] at its old value);
+    if (tid == 0) {
+        double cur = lnw[start];
+        for (int i = start; i < end; ++i) {
+            const double nxt = valid[i] ? __dadd_rn(cur, ds[i]) : lnw[i + 1];
+            ds[i] = nxt;
+            cur = nxt;
+        }
+    }
+    __syncthreads();
+    // (c) write back and normalise by lnW[0] (bin 0 is never rewritten)
+    for (uint32_t i = tid; i <= N; i += bs) {
+        double v = ((int)i > start && (int)i <= end) ? ds[i - 1] : lnw[i];
+        v = __dsub_rn(v, lnw0);
+        lnw[i] = v;
+        w32[i] = (float)v;
+    }
+}
+
+__global__ void k_run_clear(unsigned long long *hist, uint32_t n, const RunCtl *ctl)
+{
+    if (ctl->st.stop) return;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) hist[i] = 0ull;
+}
+
+__global__ void k_to_f32(const double *lnw, float *w32, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) w32[i] = (float)lnw[i];
+}
+
+static size_t update_smem(uint32_t N, int rule) { return rule == 2 ? (size_t)N * (sizeof(double) + 1) : 0; }
+
+static cudaError_t prep_update(uint32_t N, int rule)
+{
+    const size_t dyn = update_smem(N, rule);
+    if (dyn > 48 * 1024)
+        return cudaFuncSetAttribute(k_weight_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    return cudaSuccess;
+}
+
+cudaError_t launch_weight_update(const unsigned long long *hist, uint32_t N, double *lnw, float *w32, double *p_acc,
+                                 int rule, HistStatsDev *stats, cudaStream_t s)
+{
+    cudaError_t e = prep_update(N, rule);
+    if (e != cudaSuccess) return e;
+    k_weight_update<<<1, kUpdThreads, update_smem(N, rule), s>>>(hist, N, lnw, w32, p_acc, rule, stats, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_run_update(const unsigned long long *hist, double *lnw, float *w32, double *p_acc, RunCtl *ctl,
+                              cudaStream_t s, uint32_t N, int rule)
+{
+    cudaError_t e = prep_update(N, rule);
+    if (e != cudaSuccess) return e;
+    k_weight_update<<<1, kUpdThreads, update_smem(N, rule), s>>>(hist, N, lnw, w32, p_acc, rule, nullptr, ctl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_run_clear(unsigned long long *hist, uint32_t n, const RunCtl *ctl, cudaStream_t s)
+{
+    k_run_clear<<<(n + 255) / 256 < 152 ? (n + 255) / 256 : 152, 256, 0, s>>>(hist, n, ctl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weights_to_f32(const double *lnw, float *w32, uint32_t n, cudaStream_t s)
+{
+    k_to_f32<<<(n + 255) / 256, 256, 0, s>>>(lnw, w32, n);
+    return cudaGetLastError();
+}
+
+}  // namespace muca

@@ -1,0 +1,676 @@
+// muca_api.cu -- the C ABI of include/muca.h on top of the GB300 kernels.
+//
+// A context owns every device buffer of one simulation: the packed lattices
+// of all chains, per-chain E_J / E_Delta / M, the FP64 master weights and
+// the FP32 shadow the weight sweep reads, the u64 histogram(s), and the
+// device-resident run state.  All work is enqueued on the context's stream.
+#include "../../include/muca.h"
+#include "muca_device.cuh"
+#include "muca_internal.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace muca;
+
+struct muca_ctx {
+    muca_params prm{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sms = 0, max_thr_sm = 0;
+    size_t smem_optin = 0;
+    uint32_t L = 0, N = 0, WPR = 0, ndev = 1, cpd = 0, nchains = 0, rounds = 7, mode = 0, dev0 = 0;
+    SweepPlan plan{};
+    size_t lat_words = 0, hist_len = 0;
+    uint32_t *d_lat = nullptr;
+    int32_t *d_ej = nullptr, *d_edel = nullptr, *d_mag = nullptr;
+    double *d_lnw = nullptr, *d_pacc = nullptr;
+    float *d_w32 = nullptr;
+    unsigned long long *d_hist = nullptr;
+    uint32_t *d_index = nullptr, *d_naver = nullptr;
+    HistStatsDev *d_stats = nullptr, *h_stats = nullptr;
+    RunCtl *d_ctl = nullptr, *h_ctl = nullptr;
+    IterRecordDev *d_recs = nullptr;
+    size_t recs_cap = 0;
+    double *d_obs_part = nullptr, *d_obs_out = nullptr, *h_obs_out = nullptr;
+    double *d_jk = nullptr;
+    size_t jk_cap = 0;
+    int8_t *d_tmp = nullptr;
+    unsigned long long *d_bad = nullptr, *h_bad = nullptr;
+    uint64_t device_bytes = 0;
+    std::string err;
+};
+
+namespace {
+
+std::string g_create_err;
+
+muca_status fail(muca_ctx *c, muca_status st, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf; else g_create_err = buf;
+    return st;
+}
+
+#define CUDA_TRY(c, x)                                                                          \
+    do {                                                                                        \
+        cudaError_t _e = (x);                                                                   \
+        if (_e != cudaSuccess) return fail((c), MUCA_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(_e)); \
+    } while (0)
+
+template <typename T>
+cudaError_t dmalloc(muca_ctx *c, T **p, size_t n)
+{
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e == cudaSuccess) c->device_bytes += n * sizeof(T);
+    return e;
+}
+
+void free_all(muca_ctx *c)
+{
+    void *dp[] = {c->d_lat, c->d_ej, c->d_edel, c->d_mag, c->d_lnw, c->d_pacc, c->d_w32, c->d_hist,
+                  c->d_index, c->d_naver, c->d_stats, c->d_ctl, c->d_recs, c->d_obs_part, c->d_obs_out,
+                  c->d_jk, c->d_tmp, c->d_bad};
+    for (void *p : dp)
+        if (p) cudaFree(p);
+    void *hp[] = {c->h_stats, c->h_ctl, c->h_obs_out, c->h_bad};
+    for (void *p : hp)
+        if (p) cudaFreeHost(p);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+}
+
+// the host-side tables of muca_delta_multigpu.cu:157-175 (for the generic kernel)
+void build_tables(uint32_t L, std::vector<uint32_t> &naver, std::vector<uint32_t> &index)
+{
+    const uint32_t N = L * L;
+    naver.assign(4 * (size_t)N, 0);
+    index.assign(N, 0);
+    for (uint32_t i = 0; i < N; i++) {
+        int right = (int)i + 1, left = (int)i - 1, up = (int)(i + L), down = (int)i - (int)L;
+        if (right % (int)L == 0) right -= (int)L;
+        if (i % L == 0) left += (int)L;
+        if (up > (int)N - 1) up -= (int)N;
+        if (down < 0) down += (int)N;
+        naver[4 * i] = right; naver[4 * i + 1] = left; naver[4 * i + 2] = up; naver[4 * i + 3] = down;
+        index[i] = ((uint32_t)(0 == ((i / (N / 2)) % 2)) * (2 * i)) % N
+                 + ((uint32_t)(1 == ((i / (N / 2)) % 2)) * (2 * i + 1)) % N;
+    }
+}
+
+muca_status ensure_tmp(muca_ctx *c)
+{
+    if (!c->d_tmp) CUDA_TRY(c, dmalloc(c, &c->d_tmp, (size_t)c->nchains * c->N));
+    return MUCA_OK;
+}
+
+muca_status recompute_energies(muca_ctx *c)
+{
+    CUDA_TRY(c, launch_energies(c->d_lat, c->d_ej, c->d_edel, c->d_mag, c->L, c->WPR, c->plan.cpb, c->nchains,
+                                c->stream));
+    return MUCA_OK;
+}
+
+SweepArgs sweep_args(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint32_t seed_dev_mul, uint64_t therm,
+                     uint64_t nup)
+{
+    SweepArgs a{};
+    a.lat = c->d_lat;
+    a.ej = c->d_ej;
+    a.edel = c->d_edel;
+    a.mag = c->d_mag;
+    a.w = c->mode == MUCA_MODE_WEIGHT ? (const void *)c->d_w32 : (const void *)c->d_lnw;
+    a.hist = c->d_hist;
+    a.index = c->d_index;
+    a.naver = c->d_naver;
+    a.L = c->L;
+    a.N = c->N;
+    a.WPR = c->WPR;
+    a.nchains = c->nchains;
+    a.chains_per_dev = c->cpd;
+    a.seed_base = seed_base + seed_dev_mul * c->dev0;  // device dev0 + d uses base + mul*(dev0+d)
+    a.seed_dev_mul = seed_dev_mul;
+    a.iter = iter;
+    a.therm = therm;
+    a.nup = nup;
+    if (c->mode == MUCA_MODE_WEIGHT) {
+        // muca_delta_multigpu.cu:740-741
+        a.k1_mul = 2; a.k1_add = 0; a.k1_hi = 0xdecafbadu;
+        a.k3_mul = 2; a.k3_add = 50000; a.k3_hi = 0x11cafeadu;
+    } else {
+        // produce2_multigpu.cu:406-408
+        a.k1_mul = 1; a.k1_add = 0; a.k1_hi = 0xdecafbadu;
+        a.k3_mul = 1; a.k3_add = 40000; a.k3_hi = 0xdecafeadu;
+    }
+    a.dyn = nullptr;
+    return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *muca_last_error(const muca_ctx *c) { return c ? c->err.c_str() : g_create_err.c_str(); }
+
+muca_status muca_default_chains(int32_t device, uint32_t *out)
+{
+    if (!out) return fail(nullptr, MUCA_ERR_BAD_ARG, "out is NULL");
+    int thr = 0, sms = 0;
+    CUDA_TRY(nullptr, cudaDeviceGetAttribute(&thr, cudaDevAttrMaxThreadsPerMultiProcessor, device));
+    CUDA_TRY(nullptr, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    *out = (uint32_t)(thr * sms);
+    return MUCA_OK;
+}
+
+muca_status muca_create(const muca_params *p, muca_ctx **out)
+{
+    if (!p || !out) return fail(nullptr, MUCA_ERR_BAD_ARG, "params/out is NULL");
+    *out = nullptr;
+    if (p->L < 2 || p->L > 128) return fail(nullptr, MUCA_ERR_BAD_ARG, "L=%u outside 2..128", p->L);
+    if (p->mode > MUCA_MODE_PRODUCE) return fail(nullptr, MUCA_ERR_BAD_ARG, "mode=%u", p->mode);
+    const uint32_t rounds = p->rounds ? p->rounds : 7;
+    if (rounds != 7 && rounds != 10) return fail(nullptr, MUCA_ERR_BAD_ARG, "rounds=%u (7 or 10)", rounds);
+    muca_ctx *c = new muca_ctx();
+    c->prm = *p;
+    c->device = p->device;
+    c->L = p->L;
+    c->N = p->L * p->L;
+    c->WPR = (p->L + 15) / 16;
+    c->ndev = p->ndev ? p->ndev : 1;
+    c->dev0 = p->dev_offset;
+    c->rounds = rounds;
+    c->mode = p->mode;
+    auto bail = [&](muca_status st) {
+        g_create_err = c->err;
+        free_all(c);
+        delete c;
+        return st;
+    };
+#define CREATE_TRY(x)                                                                               \
+    do {                                                                                            \
+        cudaError_t _e = (x);                                                                       \
+        if (_e != cudaSuccess) { fail(c, MUCA_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(_e)); return bail(MUCA_ERR_CUDA); } \
+    } while (0)
+    CREATE_TRY(cudaSetDevice(c->device));
+    int optin = 0;
+    CREATE_TRY(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device));
+    CREATE_TRY(cudaDeviceGetAttribute(&c->max_thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, c->device));
+    CREATE_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    c->smem_optin = (size_t)optin;
+    c->cpd = p->nchains ? p->nchains : (uint32_t)(c->max_thr_sm * c->sms);
+    const uint64_t total = (uint64_t)c->cpd * c->ndev;
+    if (total == 0 || total > (1ull << 26)) {
+        fail(c, MUCA_ERR_BAD_ARG, "chains=%llu outside 1..2^26", (unsigned long long)total);
+        return bail(MUCA_ERR_BAD_ARG);
+    }
+    c->nchains = (uint32_t)total;
+    c->plan = plan_sweep((int)c->mode, (int)rounds, c->L, c->nchains, c->smem_optin, c->sms);
+    if (c->plan.smem > c->smem_optin) {
+        fail(c, MUCA_ERR_BAD_ARG, "L=%u needs %zu B of shared memory per block (device has %zu)", c->L, c->plan.smem,
+             c->smem_optin);
+        return bail(MUCA_ERR_BAD_ARG);
+    }
+    if (p->stream) {
+        c->stream = (cudaStream_t)p->stream;
+    } else {
+        CREATE_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    const uint32_t N = c->N;
+    c->lat_words = (size_t)c->plan.blocks * c->plan.cpb * c->L * c->WPR;
+    c->hist_len = c->mode == MUCA_MODE_WEIGHT ? (size_t)N + 1 : (size_t)(N + 1) * (N + 2) / 2;
+    CREATE_TRY(dmalloc(c, &c->d_lat, c->lat_words));
+    CREATE_TRY(dmalloc(c, &c->d_ej, c->nchains));
+    CREATE_TRY(dmalloc(c, &c->d_edel, c->nchains));
+    CREATE_TRY(dmalloc(c, &c->d_mag, c->nchains));
+    CREATE_TRY(dmalloc(c, &c->d_lnw, (size_t)N + 1));
+    CREATE_TRY(dmalloc(c, &c->d_pacc, (size_t)N + 1));
+    CREATE_TRY(dmalloc(c, &c->d_w32, (size_t)N + 1));
+    CREATE_TRY(dmalloc(c, &c->d_hist, c->hist_len));
+    CREATE_TRY(dmalloc(c, &c->d_stats, 1));
+    CREATE_TRY(dmalloc(c, &c->d_ctl, 1));
+    CREATE_TRY(dmalloc(c, &c->d_bad, 1));
+    CREATE_TRY(cudaMallocHost((void **)&c->h_stats, sizeof(HistStatsDev)));
+    CREATE_TRY(cudaMallocHost((void **)&c->h_ctl, sizeof(RunCtl)));
+    CREATE_TRY(cudaMallocHost((void **)&c->h_bad, sizeof(unsigned long long)));
+    CREATE_TRY(cudaMallocHost((void **)&c->h_obs_out, 4 * sizeof(double)));
+    CREATE_TRY(cudaMemsetAsync(c->d_lat, 0x55, c->lat_words * 4, c->stream));  // all spins 0
+    CREATE_TRY(cudaMemsetAsync(c->d_ej, 0, c->nchains * 4, c->stream));
+    CREATE_TRY(cudaMemsetAsync(c->d_edel, 0, c->nchains * 4, c->stream));
+    CREATE_TRY(cudaMemsetAsync(c->d_mag, 0, c->nchains * 4, c->stream));
+    CREATE_TRY(cudaMemsetAsync(c->d_lnw, 0, ((size_t)N + 1) * 8, c->stream));
+    CREATE_TRY(cudaMemsetAsync(c->d_pacc, 0, ((size_t)N + 1) * 8, c->stream));
+    CREATE_TRY(cudaMemsetAsync(c->d_w32, 0, ((size_t)N + 1) * 4, c->stream));
+    CREATE_TRY(cudaMemsetAsync(c->d_hist, 0, c->hist_len * 8, c->stream));
+    if (!c->plan.fast) {
+        std::vector<uint32_t> nv, ix;
+        build_tables(c->L, nv, ix);
+        CREATE_TRY(dmalloc(c, &c->d_index, ix.size()));
+        CREATE_TRY(dmalloc(c, &c->d_naver, nv.size()));
+        CREATE_TRY(cudaMemcpyAsync(c->d_index, ix.data(), ix.size() * 4, cudaMemcpyHostToDevice, c->stream));
+        CREATE_TRY(cudaMemcpyAsync(c->d_naver, nv.data(), nv.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    }
+    CREATE_TRY(cudaStreamSynchronize(c->stream));
+#undef CREATE_TRY
+    *out = c;
+    return MUCA_OK;
+}
+
+muca_status muca_destroy(muca_ctx *c)
+{
+    if (!c) return MUCA_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_all(c);
+    delete c;
+    return MUCA_OK;
+}
+
+muca_status muca_get_info(const muca_ctx *c, muca_info *o)
+{
+    if (!c || !o) return fail(nullptr, MUCA_ERR_BAD_ARG, "NULL argument");
+    o->L = c->L;
+    o->N = c->N;
+    o->nchains_total = c->nchains;
+    o->chains_per_block = c->plan.cpb;
+    o->blocks = c->plan.blocks;
+    o->lattice_in_smem = c->plan.lat_smem;
+    o->hist_in_smem = c->mode == MUCA_MODE_WEIGHT;
+    o->weights_in_smem = 1;
+    o->smem_bytes = (uint32_t)c->plan.smem;
+    o->sms = (uint32_t)c->sms;
+    o->device_bytes = c->device_bytes;
+    return MUCA_OK;
+}
+
+muca_status muca_init_chains(muca_ctx *c, uint32_t scheme, uint32_t jack)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    InitArgs ia{};
+    ia.rounds = 7;
+    switch (scheme) {
+    case MUCA_INIT_WEIGHT:  // muca_delta_multigpu.cu:342-347
+        ia.key0_mul = 10; ia.key0_jack_mul = 2; ia.key1 = 0xdecafbadu;
+        ia.ctr0[1] = 100; ia.ctr0[2] = 0xBADCAB1Eu; ia.ctr0[3] = 0xBADC0DEDu;
+        ia.ctr0_dev_mul[0] = 2; ia.ctr_word = 0;
+        break;
+    case MUCA_INIT_PRODUCE:  // produce2_multigpu.cu:129-134
+        ia.key0_mul = 10; ia.key1 = 0xdecafbadu;
+        ia.ctr0[1] = 100; ia.ctr0[3] = 0xBADCAFE3u;
+        ia.ctr0_dev_mul[0] = 1000; ia.ctr_word = 2;
+        break;
+    case MUCA_INIT_BASELINE:
+        ia.key0_add = 2024; ia.key1_jack_mul = 1; ia.rounds = 10; ia.chain_in_ctr = 1;
+        break;
+    case MUCA_INIT_ORDERED:
+        ia.ordered = 1;
+        break;
+    default:
+        return fail(c, MUCA_ERR_BAD_ARG, "init scheme %u", scheme);
+    }
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    // emulated device index = dev0 + chain / cpd enters the init counter
+    for (int j = 0; j < 4; ++j) ia.ctr0[j] += ia.ctr0_dev_mul[j] * c->dev0;
+    ia.chain_offset = c->dev0 * c->cpd;
+    CUDA_TRY(c, launch_init(c->d_lat, c->L, c->WPR, c->plan.cpb, c->nchains, c->cpd, jack, ia, c->stream));
+    return recompute_energies(c);
+}
+
+muca_status muca_set_lattice(muca_ctx *c, const int8_t *lat, size_t n)
+{
+    if (!c || !lat) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (n != (size_t)c->nchains * c->N) return fail(c, MUCA_ERR_BAD_ARG, "n=%zu, expected %zu", n, (size_t)c->nchains * c->N);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (muca_status st = ensure_tmp(c)) return st;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_tmp, lat, n, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(c->d_bad, 0, 8, c->stream));
+    CUDA_TRY(c, launch_validate(c->d_tmp, n, c->d_bad, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_bad, c->d_bad, 8, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (*c->h_bad) return fail(c, MUCA_ERR_BAD_ARG, "%llu lattice values outside {-1,0,1}", *c->h_bad);
+    CUDA_TRY(c, launch_pack(c->d_lat, c->d_tmp, c->L, c->WPR, c->plan.cpb, c->nchains, c->stream));
+    return recompute_energies(c);
+}
+
+muca_status muca_get_lattice(muca_ctx *c, int8_t *lat, size_t n)
+{
+    if (!c || !lat) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (n != (size_t)c->nchains * c->N) return fail(c, MUCA_ERR_BAD_ARG, "n=%zu, expected %zu", n, (size_t)c->nchains * c->N);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (muca_status st = ensure_tmp(c)) return st;
+    CUDA_TRY(c, launch_unpack(c->d_lat, c->d_tmp, c->L, c->WPR, c->plan.cpb, c->nchains, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(lat, c->d_tmp, n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MUCA_OK;
+}
+
+muca_status muca_get_chain_state(muca_ctx *c, int32_t *ej, int32_t *edel, int32_t *mag, size_t n)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    if (n != c->nchains) return fail(c, MUCA_ERR_BAD_ARG, "n=%zu, expected %u", n, c->nchains);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (ej) CUDA_TRY(c, cudaMemcpyAsync(ej, c->d_ej, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (edel) CUDA_TRY(c, cudaMemcpyAsync(edel, c->d_edel, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (mag) CUDA_TRY(c, cudaMemcpyAsync(mag, c->d_mag, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MUCA_OK;
+}
+
+muca_status muca_set_weights(muca_ctx *c, const double *lnw, size_t n)
+{
+    if (!c || !lnw) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (n != (size_t)c->N + 1) return fail(c, MUCA_ERR_BAD_ARG, "n=%zu, expected N+1=%u", n, c->N + 1);
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(lnw[i])) return fail(c, MUCA_ERR_BAD_ARG, "weight %zu is not finite", i);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_lnw, lnw, n * 8, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, launch_weights_to_f32(c->d_lnw, c->d_w32, (uint32_t)n, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MUCA_OK;
+}
+
+muca_status muca_get_weights(muca_ctx *c, double *lnw, size_t n)
+{
+    if (!c || !lnw) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (n != (size_t)c->N + 1) return fail(c, MUCA_ERR_BAD_ARG, "n=%zu, expected N+1=%u", n, c->N + 1);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemcpyAsync(lnw, c->d_lnw, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MUCA_OK;
+}
+
+static muca_status do_sweep(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint32_t seed_dev_mul, uint64_t therm,
+                            uint64_t nup, bool clear)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (clear) CUDA_TRY(c, cudaMemsetAsync(c->d_hist, 0, c->hist_len * 8, c->stream));
+    const SweepArgs a = sweep_args(c, iter, seed_base, seed_dev_mul, therm, nup);
+    CUDA_TRY(c, launch_sweep(c->plan, a, c->stream));
+    return MUCA_OK;
+}
+
+muca_status muca_sweep(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint32_t seed_dev_mul, uint64_t therm,
+                       uint64_t nup)
+{
+    return do_sweep(c, iter, seed_base, seed_dev_mul, therm, nup, true);
+}
+
+muca_status muca_sweep_accumulate(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint32_t seed_dev_mul,
+                                  uint64_t therm, uint64_t nup)
+{
+    return do_sweep(c, iter, seed_base, seed_dev_mul, therm, nup, false);
+}
+
+muca_status muca_clear_histogram(muca_ctx *c)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemsetAsync(c->d_hist, 0, c->hist_len * 8, c->stream));
+    return MUCA_OK;
+}
+
+muca_status muca_get_histogram(muca_ctx *c, uint64_t *h, size_t n)
+{
+    if (!c || !h) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (n != c->hist_len) return fail(c, MUCA_ERR_BAD_ARG, "n=%zu, expected %zu", n, c->hist_len);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemcpyAsync(h, c->d_hist, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MUCA_OK;
+}
+
+muca_status muca_set_histogram(muca_ctx *c, const uint64_t *h, size_t n)
+{
+    if (!c || !h) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (n != c->hist_len) return fail(c, MUCA_ERR_BAD_ARG, "n=%zu, expected %zu", n, c->hist_len);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_hist, h, n * 8, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MUCA_OK;
+}
+
+static void stats_out(const HistStatsDev &s, muca_hist_stats *o)
+{
+    o->start = s.start;
+    o->end = s.end;
+    o->width = s.width;
+    o->visited = s.visited;
+    o->events = s.events;
+    o->min_count = s.min_count;
+    o->d_kl = s.d_kl;
+    o->min_over_mean = s.min_over_mean;
+}
+
+static muca_status update_impl(muca_ctx *c, int rule, muca_hist_stats *st)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "weight statistics need a weight-mode context");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, rule, c->d_stats, c->stream));
+    if (!st) return MUCA_OK;  // enqueue only
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(HistStatsDev), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    stats_out(*c->h_stats, st);
+    return MUCA_OK;
+}
+
+muca_status muca_histogram_stats(muca_ctx *c, muca_hist_stats *st)
+{
+    if (!st) return fail(c, MUCA_ERR_BAD_ARG, "stats is NULL");
+    return update_impl(c, -1, st);
+}
+
+muca_status muca_update_weights(muca_ctx *c, uint32_t rule, muca_hist_stats *st)
+{
+    if (rule > MUCA_UPDATE_RECURSION) return fail(c, MUCA_ERR_BAD_ARG, "rule %u", rule);
+    return update_impl(c, (int)rule, st);
+}
+
+muca_status muca_weight_run(muca_ctx *c, const muca_run_opts *o, muca_run_result *res, muca_iter_record *recs,
+                            size_t cap)
+{
+    if (!c || !o) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "weight run needs a weight-mode context");
+    if (o->rule > MUCA_UPDATE_RECURSION) return fail(c, MUCA_ERR_BAD_ARG, "rule %u", o->rule);
+    if (o->starting_M == 0) return fail(c, MUCA_ERR_BAD_ARG, "starting_M must be >= 1");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const auto t0 = std::chrono::steady_clock::now();
+    if (o->reinit_chains) {
+        if (muca_status st = muca_init_chains(c, o->init_scheme, o->jack)) return st;
+    }
+    const uint32_t max_iter = o->max_iter ? o->max_iter : 1000000u;
+    if (cap > 0 && cap > c->recs_cap) {
+        if (c->d_recs) cudaFree(c->d_recs);
+        c->d_recs = nullptr;
+        CUDA_TRY(c, dmalloc(c, &c->d_recs, cap));
+        c->recs_cap = cap;
+    }
+    RunCtl &h = *c->h_ctl;
+    std::memset(&h, 0, sizeof h);
+    h.st.k = 0;
+    h.st.nup = o->starting_M;
+    h.st.width = 10;  // muca_delta_multigpu.cu:314
+    h.st.total_run = (unsigned long long)o->starting_M * c->nchains;
+    h.N = c->N;
+    h.nchains_total = c->nchains;
+    h.rule = o->rule;
+    h.hold = o->hold_until_full;
+    h.flat_minmean = o->flat_minmean;
+    h.max_iter = max_iter;
+    h.sched = o->nup_schedule;
+    h.mom_thr = o->min_over_mean > 0 ? o->min_over_mean : 0.5;
+    h.dkl_max = o->d_kl_max > 0 ? o->d_kl_max : 1e-4;
+    h.recs = cap ? c->d_recs : nullptr;
+    h.rec_cap = (uint32_t)cap;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->stream));
+    const uint64_t therm = o->therm ? o->therm : c->N;  // therm_coeff * N (:315-316)
+    SweepArgs a = sweep_args(c, 0, 100u, 1000u, therm, 0);  // seed SEED+1000*l (:393)
+    a.dyn = &c->d_ctl->st.k;
+    cudaEvent_t e0, e1, m0, m1;
+    CUDA_TRY(c, cudaEventCreate(&e0));
+    CUDA_TRY(c, cudaEventCreate(&e1));
+    CUDA_TRY(c, cudaEventCreate(&m0));
+    CUDA_TRY(c, cudaEventCreate(&m1));
+    std::vector<double> kms, mms;
+    double tk = 0, tm = 0, nwidth_time = -1;
+    uint32_t k_done = 0;
+    muca_status rs = MUCA_OK;
+    for (;;) {
+        // one iteration per host round trip, like the reference loop; the
+        // device decides the schedule and convergence
+        cudaError_t e = launch_run_clear(c->d_hist, (uint32_t)c->hist_len, c->d_ctl, c->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+        if (e == cudaSuccess) e = launch_sweep(c->plan, a, c->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+        if (e == cudaSuccess) e = launch_run_update(c->d_hist, c->d_lnw, c->d_w32, c->d_pacc, c->d_ctl, c->stream,
+                                                    c->N, (int)o->rule);
+        if (e == cudaSuccess) e = cudaEventRecord(m0, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h.st, &c->d_ctl->st, sizeof(IterState), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(m1, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) { rs = fail(c, MUCA_ERR_CUDA, "weight run: %s", cudaGetErrorString(e)); break; }
+        float ks = 0, ms = 0;
+        cudaEventElapsedTime(&ks, e0, e1);
+        cudaEventElapsedTime(&ms, m0, m1);
+        kms.push_back(ks);
+        mms.push_back(ms);
+        tk += ks;
+        tm += ms;
+        ++k_done;
+        if (h.st.reach && nwidth_time < 0) nwidth_time = tk;
+        if (h.st.stop) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(m0);
+    cudaEventDestroy(m1);
+    if (rs != MUCA_OK) return rs;
+    if (recs && cap) {
+        std::vector<IterRecordDev> r(std::min<size_t>(cap, k_done));
+        CUDA_TRY(c, cudaMemcpy(r.data(), c->d_recs, r.size() * sizeof(IterRecordDev), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < r.size(); ++i) {
+            recs[i].k = r[i].k;
+            recs[i].width_temp = r[i].width_temp;
+            recs[i].width = r[i].width;
+            recs[i].nupdates = r[i].nupdates;
+            recs[i].total_run = r[i].total_run;
+            recs[i].d_kl = r[i].d_kl;
+            recs[i].min_over_mean = r[i].min_over_mean;
+            recs[i].kernel_ms = kms[i];
+            recs[i].memcpy_ms = mms[i];
+        }
+    }
+    if (res) {
+        res->iterations = k_done;
+        res->converged = h.st.converged;
+        res->width_reached_iter = h.st.reach ? h.st.reach_k : 0xFFFFFFFFu;
+        res->total_run = h.st.converged ? h.st.total_run : h.st.total_run;
+        res->nwidth_step = h.st.nwidth_step;
+        res->total_kernel_s = tk * 1e-3;
+        res->total_mem_s = tm * 1e-3;
+        res->nwidth_time_s = nwidth_time < 0 ? 0 : nwidth_time * 1e-3;
+        res->wall_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return h.st.converged ? MUCA_OK : fail(c, MUCA_ERR_NOT_CONVERGED, "not converged after %u iterations", k_done);
+}
+
+muca_status muca_weight_shift(muca_ctx *c, double beta, double delta)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, launch_weight_shift(c->d_lnw, c->N, beta, delta, c->stream));
+    if (c->mode == MUCA_MODE_WEIGHT) CUDA_TRY(c, launch_weights_to_f32(c->d_lnw, c->d_w32, c->N + 1, c->stream));
+    return MUCA_OK;
+}
+
+muca_status muca_compute_observables(muca_ctx *c, double beta, double delta, muca_observables *out)
+{
+    if (!c || !out) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (c->mode != MUCA_MODE_PRODUCE) return fail(c, MUCA_ERR_STATE, "observables need a production-mode context");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (!c->d_obs_part) {
+        CUDA_TRY(c, dmalloc(c, &c->d_obs_part, observables_partials(c->N)));
+        CUDA_TRY(c, dmalloc(c, &c->d_obs_out, 4));
+    }
+    CUDA_TRY(c, launch_observables(c->d_hist, c->d_lnw, c->N, beta, delta, c->d_obs_part, c->d_obs_out, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_obs_out, c->d_obs_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    const double s = c->h_obs_out[0], m1 = c->h_obs_out[1], m2 = c->h_obs_out[2], m4 = c->h_obs_out[3];
+    out->sum = s;
+    out->m1 = m1;
+    out->m2 = m2;
+    out->m4 = m4;
+    out->m_abs = m1 / s;
+    out->chi = (m2 / s - (m1 / s) * (m1 / s)) * beta / (double)c->N;
+    out->u4 = 1.0 - (m4 / s) / (3.0 * (m2 / s) * (m2 / s));
+    return MUCA_OK;
+}
+
+muca_status muca_jackknife(muca_ctx *c, const double *x, uint32_t n, double *avg, double *err)
+{
+    if (!c || !x || !avg || !err) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (n == 0) return fail(c, MUCA_ERR_BAD_ARG, "n == 0");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (n + 2 > c->jk_cap) {
+        if (c->d_jk) cudaFree(c->d_jk);
+        c->d_jk = nullptr;
+        CUDA_TRY(c, dmalloc(c, &c->d_jk, (size_t)n + 2));
+        c->jk_cap = n + 2;
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_jk, x, n * 8, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, launch_jackknife(c->d_jk, n, c->d_jk + n, c->stream));
+    double r[2];
+    CUDA_TRY(c, cudaMemcpyAsync(r, c->d_jk + n, 16, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    *avg = r[0];
+    *err = r[1];
+    return MUCA_OK;
+}
+
+muca_status muca_philox_peak(int32_t device, uint32_t rounds, double *blocks_per_s)
+{
+    if (!blocks_per_s) return fail(nullptr, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (rounds != 7 && rounds != 10) return fail(nullptr, MUCA_ERR_BAD_ARG, "rounds=%u", rounds);
+    CUDA_TRY(nullptr, cudaSetDevice(device));
+    int sms = 0, thr = 0;
+    CUDA_TRY(nullptr, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    CUDA_TRY(nullptr, cudaDeviceGetAttribute(&thr, cudaDevAttrMaxThreadsPerMultiProcessor, device));
+    const uint32_t grid = (uint32_t)(sms * (thr / 256)), per = 4096;
+    uint32_t *out = nullptr;
+    CUDA_TRY(nullptr, cudaMalloc(&out, (size_t)grid * 256 * 4));
+    cudaStream_t s;
+    cudaEvent_t e0, e1;
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    cudaError_t err = cudaSuccess;
+    for (int rep = 0; rep < 5 && err == cudaSuccess; ++rep) {
+        cudaEventRecord(e0, s);
+        err = launch_philox_peak((int)rounds, grid, per, out, s);
+        cudaEventRecord(e1, s);
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;  // first launch is warm-up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    cudaFree(out);
+    if (err != cudaSuccess) return fail(nullptr, MUCA_ERR_CUDA, "philox peak: %s", cudaGetErrorString(err));
+    *blocks_per_s = (double)grid * 256.0 * per / (best * 1e-3);
+    return MUCA_OK;
+}
+
+}  // extern "C"

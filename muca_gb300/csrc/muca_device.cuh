@@ -1,0 +1,79 @@
+// muca_device.cuh -- device primitives shared by the GB300 kernels.
+//
+// Philox4x32-R (Salmon et al., SC'11, sec. 3.2) with the constants of
+// Random123 philox.h:232-250 and the round/key-bump order of :284-320, and the
+// u01fixedpt<float> conversion of Random123 examples/uniform.hpp:195-205.
+// Both are written here from the published algorithm; bit-exactness is
+// checked against Random123's known-answer vectors (kat_vectors:24-29).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace muca {
+
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u;
+constexpr uint32_t kPhiloxM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u;
+constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
+constexpr uint32_t kCtrTag = 0xBADC0DEDu;  // ctr.v[3] of the sweep kernels
+
+// Round keys: round r uses key + r * (W0, W1) (the key is bumped before every
+// round except the first).
+template <int R>
+struct RoundKeys {
+    uint32_t a[R], b[R];
+    __device__ __forceinline__ void init(uint32_t k0, uint32_t k1)
+    {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            a[r] = k0 + (uint32_t)r * kPhiloxW0;
+            b[r] = k1 + (uint32_t)r * kPhiloxW1;
+        }
+    }
+};
+
+template <int R>
+__device__ __forceinline__ uint4 philox(uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3, const RoundKeys<R> &k)
+{
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t hi0 = __umulhi(kPhiloxM0, x0);
+        const uint32_t lo0 = kPhiloxM0 * x0;
+        const uint32_t hi1 = __umulhi(kPhiloxM1, x2);
+        const uint32_t lo1 = kPhiloxM1 * x2;
+        x0 = hi1 ^ x1 ^ k.a[r];
+        x1 = lo1;
+        x2 = hi0 ^ x3 ^ k.b[r];
+        x3 = lo0;
+    }
+    return make_uint4(x0, x1, x2, x3);
+}
+
+__device__ __forceinline__ uint32_t pick(const uint4 &v, int i)
+{
+    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// u01fixedpt<float>(r) = (1 | (r >> 8)) * 2^-24, exact in FP32.
+__device__ __forceinline__ float u01f(uint32_t r)
+{
+    return __uint2float_rn((r >> 8) | 1u) * 5.9604644775390625e-08f;
+}
+
+// Initial spin (u < 1/3.0) + (u < 2/3.0) - 1 with the float u compared in
+// double (muca_delta_multigpu.cu:350).
+__device__ __forceinline__ int init_spin(uint32_t r)
+{
+    const double u = (double)u01f(r);
+    return (u < 1.0 / 3.0) + (u < 2.0 / 3.0) - 1;
+}
+
+// Packed lattice: 2 bits per site holding s+1 in {0,1,2}; a row of L sites is
+// stored in WPR = ceil(L/16) 32-bit words (site col at bits 2*(col%16) of
+// word col/16).  Device layout [block][row*WPR + word][lane]: the 32 lanes of
+// a warp touch 32 consecutive words, so every access is one 128-byte line.
+__device__ __forceinline__ uint32_t spin_code(uint32_t word, uint32_t col) { return (word >> (2u * (col & 15u))) & 3u; }
+
+constexpr uint32_t kZeroWord = 0x55555555u;  // sixteen spins of value 0
+
+}  // namespace muca

@@ -1,0 +1,126 @@
+// muca_internal.h -- launch interfaces between the C ABI (muca_api.cu) and the
+// kernel translation units.  Not part of the public ABI.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace muca {
+
+// One sweep launch.  The lattice is packed (see muca_device.cuh); `w` is
+// float[N+1] (weight mode) or double[N+1] (production mode); `hist` is
+// u64[N+1] or u64[(N+1)(N+2)/2].  Chain c belongs to emulated device
+// c / chains_per_dev and uses WORKER = c % chains_per_dev; its Philox keys
+// are k1 = {k1_mul*W + k1_add, k1_hi}, k3 = {k3_mul*W + k3_add, k3_hi}, its
+// counter {c0, seed_base + seed_dev_mul*dev, iter, 0xBADC0DED}.
+struct SweepArgs {
+    uint32_t *lat;
+    int32_t *ej, *edel, *mag;
+    const void *w;
+    unsigned long long *hist;
+    const uint32_t *index;  // sweep order (generic kernel only), N entries
+    const uint32_t *naver;  // neighbours (generic kernel only), 4N entries
+    uint32_t L, N, WPR, nchains, chains_per_dev;
+    uint32_t seed_base, seed_dev_mul, iter;
+    unsigned long long therm, nup;
+    uint32_t k1_mul, k1_add, k1_hi, k3_mul, k3_add, k3_hi;
+    // optional device-resident (iter, nup, skip) for graph-captured loops;
+    // when non-null they override iter/nup and a nonzero skip makes the
+    // launch a no-op.
+    const uint32_t *dyn;
+};
+
+enum SweepMode { kModeWeight = 0, kModeProduce = 1 };
+
+struct SweepPlan {
+    int mode;
+    int rounds;
+    bool fast;       // windowed kernel (L % 8 == 0) vs generic per-step kernel
+    bool lat_smem;   // lattice resident in shared memory
+    uint32_t cpb;    // chains (threads) per block
+    uint32_t blocks;
+    size_t smem;     // dynamic shared memory bytes
+};
+
+// Chooses placement and block shape for (mode, L, nchains) on a device with
+// `smem_optin` bytes of opt-in shared memory per block and `sms` SMs.
+SweepPlan plan_sweep(int mode, int rounds, uint32_t L, uint32_t nchains, size_t smem_optin, int sms);
+cudaError_t launch_sweep(const SweepPlan &p, const SweepArgs &a, cudaStream_t s);
+
+// Lattice helpers (k_lattice.cu).
+// key = {key0_mul*W + key0_jack_mul*jack + key0_add, key1 + key1_jack_mul*jack}
+struct InitArgs {
+    uint32_t key0_mul, key0_jack_mul, key0_add, key1, key1_jack_mul;
+    uint32_t ctr0[4], ctr0_dev_mul[4];
+    uint32_t ctr_word;  // counter word incremented before every 4 sites
+    uint32_t rounds;
+    uint32_t chain_in_ctr;  // 1: ctr[0] = chain_offset + chain and ctr[1] = group (baseline scheme)
+    uint32_t chain_offset;
+    uint32_t ordered;       // 1: every spin +1
+};
+cudaError_t launch_init(uint32_t *lat, uint32_t L, uint32_t WPR, uint32_t cpb, uint32_t nchains,
+                        uint32_t chains_per_dev, uint32_t jack, const InitArgs &ia, cudaStream_t s);
+cudaError_t launch_pack(uint32_t *lat, const int8_t *src, uint32_t L, uint32_t WPR, uint32_t cpb,
+                        uint32_t nchains, cudaStream_t s);
+cudaError_t launch_unpack(const uint32_t *lat, int8_t *dst, uint32_t L, uint32_t WPR, uint32_t cpb,
+                          uint32_t nchains, cudaStream_t s);
+cudaError_t launch_energies(const uint32_t *lat, int32_t *ej, int32_t *edel, int32_t *mag, uint32_t L,
+                            uint32_t WPR, uint32_t cpb, uint32_t nchains, cudaStream_t s);
+// Checks that every value of an int8 lattice is in {-1,0,1}; *bad gets the count of others.
+cudaError_t launch_validate(const int8_t *src, size_t n, unsigned long long *bad, cudaStream_t s);
+
+// Weight math (k_weights.cu), FP64, one block per instance.
+struct HistStatsDev {
+    int32_t start, end;
+    uint32_t width, visited;
+    unsigned long long events, min_count;
+    double d_kl, min_over_mean;
+};
+// stats of hist[0..N]; if rule >= 0 also updates lnw (FP64) / w32 (FP32 shadow)
+// (rule: 0 trivial, 1 trivial-cpu, 2 recursion with p_acc).
+cudaError_t launch_weight_update(const unsigned long long *hist, uint32_t N, double *lnw, float *w32,
+                                 double *p_acc, int rule, HistStatsDev *stats, cudaStream_t s);
+
+// Device-resident state of a weight-estimation run (the loop of
+// muca_delta_multigpu.cu:374-477).  The first three words are what the
+// sweep kernel reads through SweepArgs::dyn: iteration index, NUPDATES of
+// this iteration, stop flag.
+struct IterState {
+    uint32_t k, nup, stop, width;
+    uint32_t reach, reach_k, converged, width_temp;
+    unsigned long long total_run, nwidth_step;
+};
+struct IterRecordDev {
+    uint32_t k, width_temp, width, nupdates;
+    unsigned long long total_run;
+    double d_kl, min_over_mean;
+};
+struct RunCtl {
+    IterState st;
+    uint32_t N, nchains_total, rule, hold, flat_minmean, max_iter, sched, rec_cap;
+    double mom_thr, dkl_max;
+    IterRecordDev *recs;
+};
+// One iteration's tail: statistics, width/convergence bookkeeping, weight
+// update, schedule of the next NUPDATES; a no-op once st.stop is set.
+cudaError_t launch_run_update(const unsigned long long *hist, double *lnw, float *w32, double *p_acc,
+                              RunCtl *ctl, cudaStream_t s, uint32_t N, int rule);
+// Clears the weight histogram unless the run has stopped.
+cudaError_t launch_run_clear(unsigned long long *hist, uint32_t n, const RunCtl *ctl, cudaStream_t s);
+cudaError_t launch_weights_to_f32(const double *lnw, float *w32, uint32_t n, cudaStream_t s);
+
+// Production reweighting (k_observables.cu).
+cudaError_t launch_weight_shift(double *lnw, uint32_t N, double beta, double delta, cudaStream_t s);
+// Sums {sum, M1, M2, M4} over the triangular histogram with boltz_i =
+// exp(-beta*delta*i - lnw_i) into out[4] (device), using `partials`
+// (device, at least observables_partials(N) doubles) as scratch.
+size_t observables_partials(uint32_t N);
+cudaError_t launch_observables(const unsigned long long *hist2d, const double *lnw, uint32_t N, double beta,
+                               double delta, double *partials, double *out, cudaStream_t s);
+cudaError_t launch_jackknife(const double *x, uint32_t n, double *out2, cudaStream_t s);
+
+// Philox throughput microbenchmark (k_bench.cu): grid blocks of 256 threads,
+// each generating blocks_per_thread Philox4x32-R blocks.
+cudaError_t launch_philox_peak(int rounds, uint32_t grid, uint32_t blocks_per_thread, uint32_t *out, cudaStream_t s);
+
+}  // namespace muca

@@ -1,0 +1,45 @@
+"""Shared test set-up.
+
+Markers: `gpu` marks tests that need a CUDA device (run with -m gpu on a
+GB300); everything else runs on a CPU-only machine.
+"""
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); run with -m gpu")
+
+
+@pytest.fixture(scope="session")
+def orc():
+    from oracle import orc as o
+    o.build()
+    return o
+
+
+@pytest.fixture(scope="session")
+def muca():
+    """The engine, built for sm_103a; GPU tests only."""
+    from muca_gb300 import build as b
+    b.build()
+    import muca_gb300
+    muca_gb300.lib()
+    return muca_gb300
+
+
+@pytest.fixture(scope="session")
+def refgpu(orc):
+    """Launcher of the reference kernels (cubins compiled from the reference
+    sources); None when the cubins are not present in this checkout."""
+    try:
+        orc.build(refgpu=True)
+    except Exception:
+        return None
+    return orc.refgpu()

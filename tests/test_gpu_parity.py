@@ -1,0 +1,399 @@
+"""GPU parity: the sm_103a kernels against the CPU oracle and against the
+reference's own kernels (muca_delta_multigpu.cu / produce2_multigpu.cu
+compiled unchanged into cubins and launched through oracle/refgpu.cpp).
+
+Integer results (lattices, E_J, E_Delta, M, histograms) must be bit-exact;
+FP64 weights within 1e-12 relative (1e-9 absolute near zero); observables
+within 1e-12 relative.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SEED = 100
+
+
+def _weights(N, rng, sigma=1.5):
+    # a log-weight whose differences straddle the Metropolis threshold
+    return np.cumsum(rng.normal(0.0, sigma, N + 1)) * 0.5
+
+
+def _oracle_weight_sweep(orc, L, lat, ej, ed, w32, it, therm, nup, ndev, cpd, rounds=7):
+    """the oracle over `ndev` emulated devices of `cpd` chains each"""
+    N = L * L
+    lat = lat.copy()
+    ej = ej.copy()
+    ed = ed.copy()
+    h = np.zeros(N + 1, np.uint64)
+    for d in range(ndev):
+        sl = slice(d * cpd, (d + 1) * cpd)
+        sub, _ = orc.weight_sweep(L, lat[sl], ej[sl], ed[sl], w32, it, SEED + 1000 * d, therm, nup,
+                                  chain0=0, rounds=rounds, nthreads=8, hist=h)
+        lat[sl] = sub
+    return lat, ej, ed, h
+
+
+def _ej_ed_copy(a):
+    return np.ascontiguousarray(a, np.int32).copy()
+
+
+@pytest.mark.parametrize("L,cpd,ndev,jack", [(4, 256, 1, 0), (6, 100, 2, 1), (8, 256, 1, 3), (16, 300, 2, 0),
+                                             (72, 64, 1, 2), (10, 33, 3, 0)])
+def test_init_weight_scheme(muca, orc, L, cpd, ndev, jack):
+    with muca.Engine(L, nchains=cpd, ndev=ndev) as e:
+        e.init_chains(muca.INIT_WEIGHT, jack)
+        lat = e.get_lattice()
+        ej, ed, mg = e.chain_state()
+    exp = np.concatenate([orc.init_lattice(L, cpd, orc.scheme_weight(jack, d)) for d in range(ndev)])
+    np.testing.assert_array_equal(lat, exp)
+    oj, od, om = orc.energies(L, exp)
+    np.testing.assert_array_equal(ej, oj)
+    np.testing.assert_array_equal(ed, od)
+    np.testing.assert_array_equal(mg, om)
+
+
+@pytest.mark.parametrize("L,cpd,ndev", [(4, 256, 2), (16, 100, 1), (24, 64, 1)])
+def test_init_produce_scheme(muca, orc, L, cpd, ndev):
+    with muca.Engine(L, nchains=cpd, ndev=ndev, mode=muca.MODE_PRODUCE) as e:
+        e.init_chains(muca.INIT_PRODUCE, 0)
+        lat = e.get_lattice()
+    exp = np.concatenate([orc.init_lattice(L, cpd, orc.scheme_produce(d)) for d in range(ndev)])
+    np.testing.assert_array_equal(lat, exp)
+
+
+def test_set_get_lattice_roundtrip(muca, orc):
+    rng = np.random.default_rng(5)
+    for L in (3, 16, 72):
+        with muca.Engine(L, nchains=70) as e:
+            lat = rng.integers(-1, 2, (70, L * L)).astype(np.int8)
+            e.set_lattice(lat)
+            np.testing.assert_array_equal(e.get_lattice(), lat)
+            oj, od, om = orc.energies(L, lat)
+            ej, ed, mg = e.chain_state()
+            np.testing.assert_array_equal(ej, oj)
+            np.testing.assert_array_equal(ed, od)
+            np.testing.assert_array_equal(mg, om)
+            bad = lat.copy()
+            bad[3, 5] = 2
+            with pytest.raises(muca.MucaError):
+                e.set_lattice(bad)
+
+
+# (L, chains per device, emulated devices, therm, nup): fast kernel for L % 8 == 0,
+# generic kernel otherwise; partial windows, sweep wrap-around, therm only, nup only
+SWEEPS = [
+    (8, 256, 1, 64, 1), (8, 256, 1, 64, 13), (16, 200, 2, 256, 1000), (24, 96, 1, 0, 3 * 576 + 5),
+    (72, 64, 1, 5184, 37), (72, 40, 2, 100, 5184 + 9), (32, 128, 1, 1024, 0),
+    (4, 256, 1, 16, 333), (6, 100, 2, 36, 77), (10, 64, 1, 100, 250), (2, 40, 1, 4, 50), (3, 32, 1, 9, 41),
+]
+
+
+@pytest.mark.parametrize("L,cpd,ndev,therm,nup", SWEEPS)
+def test_weight_sweep_vs_oracle(muca, orc, L, cpd, ndev, therm, nup):
+    rng = np.random.default_rng(L * 1000 + nup)
+    N = L * L
+    lnw = _weights(N, rng)
+    it = int(rng.integers(0, 50))
+    with muca.Engine(L, nchains=cpd, ndev=ndev) as e:
+        e.set_weights(lnw)
+        e.init_chains(muca.INIT_WEIGHT, 1)
+        lat0 = e.get_lattice()
+        ej0, ed0, _ = e.chain_state()
+        e.sweep(it, SEED, 1000, therm, nup)
+        lat1 = e.get_lattice()
+        ej1, ed1, _ = e.chain_state()
+        h = e.histogram()
+    olat, oej, oed, oh = _oracle_weight_sweep(orc, L, lat0, _ej_ed_copy(ej0), _ej_ed_copy(ed0),
+                                              lnw.astype(np.float32), it, therm, nup, ndev, cpd)
+    np.testing.assert_array_equal(lat1, olat)
+    np.testing.assert_array_equal(ed1, oed)
+    np.testing.assert_array_equal(ej1, oej)
+    np.testing.assert_array_equal(h, oh)
+    assert int(h.sum()) == cpd * ndev * nup
+
+
+@pytest.mark.parametrize("L,therm,nup", [(8, 64, 500), (16, 256, 300), (24, 576, 100), (72, 5184, 41),
+                                         (4, 16, 200), (6, 36, 99), (10, 100, 57)])
+def test_weight_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup):
+    if refgpu is None:
+        pytest.skip("reference cubins not present in this checkout")
+    rng = np.random.default_rng(L + 7)
+    N = L * L
+    lnw = _weights(N, rng)
+    w32 = lnw.astype(np.float32)
+    it = 3
+    with muca.Engine(L, nchains=256) as e:
+        e.set_weights(lnw)
+        e.init_chains(muca.INIT_WEIGHT, 0)
+        lat0 = e.get_lattice()
+        ej0, ed0, _ = e.chain_state()
+        e.sweep(it, SEED, 1000, therm, nup)
+        lat1 = e.get_lattice()
+        ej1, ed1, _ = e.chain_state()
+        h = e.histogram()
+    rl, rh, rej, red, _ = orc.refgpu_weight(L, lat0, w32, ej0, ed0, it, SEED, therm, nup)
+    np.testing.assert_array_equal(lat1, rl)
+    np.testing.assert_array_equal(ed1, red)
+    np.testing.assert_array_equal(ej1, rej)
+    np.testing.assert_array_equal(h, rh)
+
+
+def test_reference_kernel_init_energies(muca, orc, refgpu):
+    """computeEnergies/computeDeltaE of the reference against ours."""
+    if refgpu is None:
+        pytest.skip("reference cubins not present in this checkout")
+    L = 16
+    with muca.Engine(L, nchains=256) as e:
+        e.init_chains(muca.INIT_WEIGHT, 0)
+        lat0 = e.get_lattice()
+        ej0, ed0, _ = e.chain_state()
+    w32 = np.zeros(L * L + 1, np.float32)
+    _, _, rej, red, _ = orc.refgpu_weight(L, lat0, w32, ej0 * 0, ed0 * 0, 0, SEED, 0, 0, compute_energies=True)
+    np.testing.assert_array_equal(rej, ej0)
+    np.testing.assert_array_equal(red, ed0)
+
+
+@pytest.mark.parametrize("rounds", [7, 10])
+def test_weight_sweep_rounds(muca, orc, rounds):
+    L, cpd = 16, 96
+    rng = np.random.default_rng(rounds)
+    lnw = _weights(L * L, rng)
+    with muca.Engine(L, nchains=cpd, rounds=rounds) as e:
+        e.set_weights(lnw)
+        e.init_chains(muca.INIT_WEIGHT, 0)
+        lat0 = e.get_lattice()
+        ej0, ed0, _ = e.chain_state()
+        e.sweep(1, SEED, 1000, 256, 700)
+        lat1 = e.get_lattice()
+        h = e.histogram()
+    olat, _, _, oh = _oracle_weight_sweep(orc, L, lat0, _ej_ed_copy(ej0), _ej_ed_copy(ed0), lnw.astype(np.float32),
+                                          1, 256, 700, 1, cpd, rounds=rounds)
+    np.testing.assert_array_equal(lat1, olat)
+    np.testing.assert_array_equal(h, oh)
+
+
+@pytest.mark.parametrize("L,cpd,therm,nup", [(8, 256, 64, 300), (16, 200, 0, 1000), (4, 100, 16, 123),
+                                             (24, 64, 576, 50), (6, 64, 0, 200)])
+def test_produce_sweep_vs_oracle(muca, orc, L, cpd, therm, nup):
+    rng = np.random.default_rng(L * 7 + nup)
+    N = L * L
+    lnw = _weights(N, rng)
+    with muca.Engine(L, nchains=cpd, mode=muca.MODE_PRODUCE) as e:
+        e.set_weights(lnw)
+        e.init_chains(muca.INIT_PRODUCE, 0)
+        lat0 = e.get_lattice()
+        ej0, ed0, mg0 = e.chain_state()
+        e.sweep(5, SEED, 2000, therm, nup)
+        lat1 = e.get_lattice()
+        ej1, ed1, mg1 = e.chain_state()
+        h = e.histogram()
+    a = lat0.copy()
+    oej, oed, omg = _ej_ed_copy(ej0), _ej_ed_copy(ed0), _ej_ed_copy(mg0)
+    olat, oh = orc.produce_sweep(L, a, oej, oed, omg, lnw, 5, SEED, therm, nup, nthreads=8)
+    np.testing.assert_array_equal(lat1, olat)
+    np.testing.assert_array_equal(ed1, oed)
+    np.testing.assert_array_equal(ej1, oej)
+    np.testing.assert_array_equal(mg1, omg)
+    np.testing.assert_array_equal(h, oh)
+
+
+@pytest.mark.parametrize("L,therm,nup", [(8, 64, 300), (16, 256, 200), (4, 0, 150), (6, 36, 100)])
+def test_produce_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup):
+    if refgpu is None:
+        pytest.skip("reference cubins not present in this checkout")
+    rng = np.random.default_rng(L * 3 + 1)
+    N = L * L
+    lnw = _weights(N, rng)
+    with muca.Engine(L, nchains=256, mode=muca.MODE_PRODUCE) as e:
+        e.set_weights(lnw)
+        e.init_chains(muca.INIT_PRODUCE, 0)
+        lat0 = e.get_lattice()
+        ej0, ed0, mg0 = e.chain_state()
+        e.sweep(2, SEED, 2000, therm, nup)
+        lat1 = e.get_lattice()
+        ej1, ed1, mg1 = e.chain_state()
+        h = e.histogram()
+    rl, rh, rej, red, rmg, _ = orc.refgpu_produce(L, lat0, lnw, ej0, ed0, mg0, 2, SEED, therm, nup)
+    np.testing.assert_array_equal(lat1, rl)
+    np.testing.assert_array_equal(ed1, red)
+    np.testing.assert_array_equal(ej1, rej)
+    np.testing.assert_array_equal(mg1, rmg)
+    np.testing.assert_array_equal(h, rh)
+
+
+def test_sweep_accumulate_and_determinism(muca):
+    L = 16
+    outs = []
+    for _ in range(2):
+        with muca.Engine(L, nchains=128) as e:
+            e.init_chains(muca.INIT_WEIGHT, 0)
+            e.sweep(0, SEED, 1000, 256, 100)
+            h1 = e.histogram()
+            e.sweep(1, SEED, 1000, 0, 50, accumulate=True)
+            h2 = e.histogram()
+            outs.append((h1, h2, e.get_lattice()))
+    assert int(outs[0][0].sum()) == 128 * 100 and int(outs[0][1].sum()) == 128 * 150
+    for a, b in zip(outs[0], outs[1]):
+        np.testing.assert_array_equal(a, b)
+
+
+# ---- FP64 weight math on the device --------------------------------------------------------
+
+def _rand_hist(rng, N, zeros=0.2):
+    h = rng.integers(0, 5000, N + 1).astype(np.uint64)
+    h[rng.random(N + 1) < zeros] = 0
+    h[: 2] = [0, 1]
+    return h
+
+
+@pytest.mark.parametrize("N", [16, 64, 5184, 16384])
+def test_hist_stats_vs_oracle(muca, orc, N):
+    L = int(round(N ** 0.5))
+    rng = np.random.default_rng(N)
+    h = _rand_hist(rng, N)
+    with muca.Engine(L, nchains=32) as e:
+        e.set_histogram(h)
+        s = e.hist_stats()
+    assert (s.start, s.end) == orc.hist_range(h)
+    assert s.width == s.end - s.start
+    assert s.visited == int((h > 0).sum()) and s.events == int(h.sum()) and s.min_count == int(h.min())
+    np.testing.assert_allclose(s.d_kl, orc.kull_leibler(h), rtol=1e-12)
+    np.testing.assert_allclose(s.min_over_mean, orc.flatness(h), rtol=1e-14)
+
+
+@pytest.mark.parametrize("rule", [0, 1, 2])
+@pytest.mark.parametrize("N", [64, 5184])
+def test_weight_update_vs_oracle(muca, orc, rule, N):
+    L = int(round(N ** 0.5))
+    rng = np.random.default_rng(N + rule)
+    Lb = orc.lib()
+    with muca.Engine(L, nchains=32) as e:
+        lnw = rng.normal(0, 10, N + 1)
+        pacc = np.zeros(N + 1)
+        e.set_weights(lnw)
+        ref = lnw.copy()
+        for step in range(3):  # p_acc persists across updates
+            h = _rand_hist(rng, N, zeros=0.05 if step else 0.3)
+            e.set_histogram(h)
+            e.update_weights(rule)
+            if rule == 0:
+                Lb.orc_update_trivial_gpu(h, N, ref)
+            elif rule == 1:
+                Lb.orc_update_trivial_cpu(h, N, ref)
+            else:
+                s, en = orc.hist_range(h)
+                Lb.orc_weight_recursion(h, N, pacc, s, en, ref)
+                ref -= ref[0]
+            got = e.get_weights()
+            np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-9)
+
+
+@pytest.mark.parametrize("rule,hold,flat", [(0, 0, 0), (2, 0, 0), (0, 1, 0), (0, 0, 1), (1, 0, 0)])
+def test_weight_run_vs_oracle(muca, orc, rule, hold, flat):
+    """Whole reference iteration loop (schedule, width, D_KL, update) on the
+    device against orc_weight_run, iteration by iteration."""
+    L, cpd, max_iter = 8, 256, 60
+    N = L * L
+    with muca.Engine(L, nchains=cpd) as e:
+        res, recs = e.weight_run(starting_M=1, jack=0, rule=rule, hold_until_full=hold, flat_minmean=flat,
+                                 max_iter=max_iter, records=max_iter)
+        lat = e.get_lattice()
+        w = e.get_weights()
+    if rule == 1:
+        pytest.skip("the CPU-flavour update has no oracle run loop; covered by test_weight_update_vs_oracle")
+    o = orc.WeightOpts(L=L, nchains=cpd, jack=0, gpu=0, starting_M=1, recursive=1 if rule == 2 else 0,
+                       hold_until_full=hold, flat_minmean=flat, max_iter=max_iter, rounds=7, nthreads=8)
+    olat = orc.init_lattice(L, cpd, orc.scheme_weight(0, 0)).reshape(-1).copy()
+    oej, oed, _ = orc.energies(L, olat.reshape(cpd, N))
+    lnw = np.zeros(N + 1)
+    pacc = np.zeros(N + 1)
+    rec = np.zeros(5 * max_iter)
+    conv = ctypes.c_int()
+    it = orc.lib().orc_weight_run(ctypes.byref(o), olat, oej, oed, lnw, pacc, rec, max_iter, ctypes.byref(conv))
+    assert res.iterations == it
+    assert res.converged == conv.value
+    rec = rec.reshape(max_iter, 5)
+    for k, r in enumerate(recs):
+        assert r.width_temp == int(rec[k, 0]), k
+        assert r.nupdates == int(rec[k, 2]), k
+        assert r.total_run == int(rec[k, 3]), k
+        np.testing.assert_allclose(r.d_kl, rec[k, 1], rtol=1e-10, atol=1e-15)
+        np.testing.assert_allclose(r.min_over_mean, rec[k, 4], rtol=1e-12)
+    np.testing.assert_array_equal(lat, olat.reshape(cpd, N))
+    np.testing.assert_allclose(w, lnw, rtol=1e-12, atol=1e-9)
+
+
+# ---- production reweighting ----------------------------------------------------------------
+
+@pytest.mark.parametrize("L,delta", [(4, 1.96), (8, 1.5), (16, 1.99)])
+def test_observables_vs_oracle(muca, orc, L, delta):
+    N = L * L
+    beta = 2.0
+    rng = np.random.default_rng(L)
+    hs = (N + 1) * (N + 2) // 2
+    h = rng.integers(0, 10000, hs).astype(np.uint64)
+    h[rng.random(hs) < 0.4] = 0
+    lnw = np.cumsum(rng.normal(-1.0, 0.5, N + 1))
+    with muca.Engine(L, nchains=64, mode=muca.MODE_PRODUCE) as e:
+        e.set_weights(lnw)
+        e.set_histogram(h)
+        e.weight_shift(beta, delta)
+        shifted = e.get_weights()
+        ob = e.observables(beta, delta)
+    ref = lnw.copy()
+    orc.lib().orc_weight_shift(beta, delta, N, ref)
+    np.testing.assert_array_equal(shifted, ref)
+    bz = np.zeros(N + 1)
+    orc.lib().orc_boltz(beta, delta, N, ref, bz, 0)
+    o = orc.observables(beta, N, h, bz)
+    np.testing.assert_allclose([ob.m_abs, ob.chi, ob.u4], o[:3], rtol=1e-12)
+    np.testing.assert_allclose([ob.sum, ob.m1, ob.m2, ob.m4], o[3:], rtol=1e-12)
+
+
+def test_jackknife_vs_oracle(muca, orc):
+    rng = np.random.default_rng(1)
+    with muca.Engine(8, nchains=32) as e:
+        for J in (1, 2, 5, 10, 37):
+            x = rng.normal(2.0, 0.3, J)
+            a, s = e.jackknife(x)
+            oa, os_ = orc.jackknife(x)
+            np.testing.assert_allclose(a, oa, rtol=1e-15)
+            if J == 1:
+                assert np.isnan(s) and np.isnan(os_)
+            else:
+                np.testing.assert_allclose(s, os_, rtol=1e-13)
+
+
+# ---- full-size workload (L=72, 16384 chains) -------------------------------------------------
+
+def test_full_size_L72_properties(muca, orc):
+    """The benchmark workload: every chain's final E_Delta / E_J is
+    consistent with its lattice, the histogram holds exactly chains*nup
+    entries, and a subset of chains matches the oracle bit for bit."""
+    L, nch = 72, 16384
+    N = L * L
+    rng = np.random.default_rng(72)
+    lnw = _weights(N, rng, sigma=0.8)
+    with muca.Engine(L, nchains=nch) as e:
+        assert e.info.lattice_in_smem == 1
+        e.set_weights(lnw)
+        e.init_chains(muca.INIT_WEIGHT, 0)
+        lat0 = e.get_lattice()
+        ej0, ed0, _ = e.chain_state()
+        e.sweep(7, SEED, 1000, N, 2 * N + 8)
+        lat1 = e.get_lattice()
+        ej1, ed1, mg1 = e.chain_state()
+        h = e.histogram()
+    assert int(h.sum()) == nch * (2 * N + 8)
+    oj, od, om = orc.energies(L, lat1)
+    np.testing.assert_array_equal(ej1, oj)
+    np.testing.assert_array_equal(ed1, od)
+    for lo, hi in ((0, 48), (8190, 8200), (nch - 40, nch)):
+        a = lat0[lo:hi].copy()
+        ej, ed = _ej_ed_copy(ej0[lo:hi]), _ej_ed_copy(ed0[lo:hi])
+        orc.weight_sweep(L, a, ej, ed, lnw.astype(np.float32), 7, SEED, N, 2 * N + 8, chain0=lo, nthreads=8)
+        np.testing.assert_array_equal(lat1[lo:hi], a.reshape(hi - lo, N))
+        np.testing.assert_array_equal(ed1[lo:hi], ed)
