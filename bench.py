@@ -347,7 +347,9 @@ def ours_arm(args, ws, rank, local):
 def ref_gpu_kernel_rate(L, chains):
     """The reference weight kernel (muca_delta_multigpu.cu:737-829, compiled
     unchanged for sm_103a) on the same step, at the config's chain count and
-    at the reference's own default (maxThreadsPerSM * SMs)."""
+    at the reference's own default (maxThreadsPerSM * SMs).  Spins come from
+    the reference initialisation (our device init, which equals it); the
+    reference's own init kernels form E_J and E_Delta."""
     try:
         import numpy as np
         from oracle import orc
@@ -359,10 +361,12 @@ def ref_gpu_kernel_rate(L, chains):
         res = {"unit": "attempts/ns", "step": "therm=N + nup=N attempts per chain, one launch"}
         for label, nw in (("config_chains", chains), ("reference_default_chains", m.default_chains(0))):
             nw = nw // 256 * 256
-            lat = orc.init_lattice(L, nw, orc.scheme_weight(0, 0))
-            ej, ed, _ = orc.energies(L, lat)
+            with m.Engine(L, nchains=nw) as e:
+                e.init_chains(m.INIT_WEIGHT, 0)
+                lat = e.get_lattice()
+            z = np.zeros(nw, np.int32)
             w32 = np.zeros(N + 1, np.float32)
-            orc.refgpu_weight(L, lat, w32, ej, ed, 0, 100, N, 0)  # warm-up (load, first launch)
+            lat, _, ej, ed, _ = orc.refgpu_weight(L, lat, w32, z, z, 0, 100, N, 0, compute_energies=True)
             _, _, _, _, ms = orc.refgpu_weight(L, lat, w32, ej, ed, 1, 100, N, N)
             res[label] = {"chains": nw, "value": nw * 2 * N / (ms * 1e6), "ms": ms}
         return res

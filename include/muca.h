@@ -87,6 +87,8 @@ typedef struct muca_info {
     uint32_t L, N, nchains_total, chains_per_block, blocks, lattice_in_smem, hist_in_smem;
     uint32_t smem_bytes, sms, weights_in_smem;
     uint64_t device_bytes;
+    double log_bracket;  /* bound used by the fast acceptance test: twice the measured
+                            max |__logf(u) - logf(u)| over all u01fixedpt<float> values */
 } muca_info;
 
 /* Histogram summary (muca_delta_multigpu.cu:431-447 and the min/mean test of

@@ -51,7 +51,7 @@ class Info(C.Structure):
     _fields_ = [("L", C.c_uint32), ("N", C.c_uint32), ("nchains_total", C.c_uint32),
                 ("chains_per_block", C.c_uint32), ("blocks", C.c_uint32), ("lattice_in_smem", C.c_uint32),
                 ("hist_in_smem", C.c_uint32), ("smem_bytes", C.c_uint32), ("sms", C.c_uint32),
-                ("weights_in_smem", C.c_uint32), ("device_bytes", C.c_uint64)]
+                ("weights_in_smem", C.c_uint32), ("device_bytes", C.c_uint64), ("log_bracket", C.c_double)]
 
 
 class HistStats(C.Structure):

@@ -19,16 +19,24 @@
 //   * the sweep is processed in windows of the 8 (or 4) same-parity sites of
 //     one word of one row.  Sites of a window are never neighbours of each
 //     other (their neighbours are the other parity or the rows above/below),
-//     so the whole window's proposals, energy changes and logf(u) are formed
-//     from four word loads with full instruction-level parallelism; only the
+//     so the whole window's proposals and energy changes are formed from four
+//     word loads with nibble-parallel (SWAR) arithmetic; only the
 //     accept/reject scan over E_Delta is sequential.  The window's new spins
-//     are merged into one word store.
+//     are merged into one word store;
+//   * the acceptance test uses the hardware __logf(u) and falls back to the
+//     exact logf(u) (replaying the window) whenever __logf(u) lies within the
+//     measured worst-case difference of the two functions from diff in any
+//     lane, so every decision equals the reference's logf decision;
+//   * the Philox blocks of the next window are generated while the current
+//     window's sequential scan runs (a two-group queue), so the integer work
+//     fills the latency of the scan.
 // The generic kernel (any L) follows the reference step by step on the same
 // packed layout and is used for L % 8 != 0.
 #include "muca_device.cuh"
 #include "muca_internal.h"
 
 #include <algorithm>
+#include <cstring>
 
 namespace muca {
 
@@ -51,21 +59,65 @@ __host__ __device__ inline size_t smem_hist_bytes(int mode, uint32_t N)
 
 struct ChainState {
     int E, EJ, M;
-    uint32_t c0;
 };
 
-// One window: SLOTS consecutive attempts on the same-parity (HALF) sites of
-// word q of row `row`; `len` <= SLOTS of them are performed (fewer only at
-// the end of a phase).  lat points at this lane's word 0 with stride cpb.
+// Random numbers of one group of four attempts: one Philox block of the
+// acceptance stream (k1) and one of the direction stream (k3) at the same
+// counter, as the reference draws them (muca_delta_multigpu.cu:794-797).
+struct Group {
+    uint32_t r1[4], r3[4];
+};
+
+template <int R>
+__device__ __forceinline__ Group gen_group(uint32_t cc, uint32_t seed, uint32_t iter, const RoundKeys<R> &k1,
+                                           const RoundKeys<R> &k3)
+{
+    const uint4 a = philox<R>(cc, seed, iter, kCtrTag, k1);
+    const uint4 b = philox<R>(cc, seed, iter, kCtrTag, k3);
+    Group g;
+    g.r1[0] = a.x; g.r1[1] = a.y; g.r1[2] = a.z; g.r1[3] = a.w;
+    g.r3[0] = b.x; g.r3[1] = b.y; g.r3[2] = b.z; g.r3[3] = b.w;
+    return g;
+}
+
+// Prefetched groups: q0 serves the next four attempts, q1 the four after;
+// qc is the counter value of q1.  The counter word 0 runs on from the
+// thermalisation into the production phase, as in the reference kernel,
+// so the queue simply carries over.
+struct Queue {
+    Group q0, q1;
+    uint32_t qc;
+};
+
+template <int R>
+__device__ __forceinline__ void refill(Queue &Q, uint32_t consumed, uint32_t seed, uint32_t iter,
+                                       const RoundKeys<R> &k1, const RoundKeys<R> &k3)
+{
+    if (consumed == 2) {
+        Q.q0 = gen_group<R>(Q.qc + 1u, seed, iter, k1, k3);
+        Q.q1 = gen_group<R>(Q.qc + 2u, seed, iter, k1, k3);
+        Q.qc += 2u;
+    } else {
+        Q.q0 = Q.q1;
+        Q.q1 = gen_group<R>(Q.qc + 1u, seed, iter, k1, k3);
+        Q.qc += 1u;
+    }
+}
+
+// One full window: the SLOTS same-parity (HALF) sites of word q of row `row`,
+// SLOTS consecutive attempts of the sweep.  lat points at this lane's word 0
+// (stride cpb).  `eps` bounds |__logf(u) - logf(u)| over every value u that
+// u01fixedpt<float> can produce (measured on the device at context creation).
 template <int MODE, int R, int SLOTS, int HALF>
 __device__ __forceinline__ void window(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
-                                       uint32_t row, uint32_t q, uint32_t len, bool rec,
+                                       uint32_t row, uint32_t q, bool rec,
                                        const typename WeightType<MODE>::T *__restrict__ wS,
                                        uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
-                                       ChainState &st, uint32_t seed, uint32_t iter, const RoundKeys<R> &k1,
-                                       const RoundKeys<R> &k3)
+                                       ChainState &st, Queue &Q, uint32_t seed, uint32_t iter, const RoundKeys<R> &k1,
+                                       const RoundKeys<R> &k3, typename WeightType<MODE>::T eps)
 {
     using WT = typename WeightType<MODE>::T;
+    constexpr uint32_t M2 = 0x33333333u;
     const uint32_t rup = (row + 1 == L) ? 0u : row + 1;
     const uint32_t rdn = (row == 0) ? L - 1 : row - 1;
     uint32_t *pc = lat + (size_t)(row * WPR + q) * cpb;
@@ -84,83 +136,172 @@ __device__ __forceinline__ void window(uint32_t *__restrict__ lat, uint32_t cpb,
     }
     const uint32_t sv = spin_code(lat[(size_t)(row * WPR + sq) * cpb], sb);
 
-    // random numbers: one pair of Philox blocks per group of 4 attempts
+    // Nibble t of `ctr` holds the spin code of the window's site t; nibble t
+    // of `nbs` the sum of its four neighbours' codes (0..8, no carries).
+    uint32_t ctr, nbs;
+    if (HALF == 0) {
+        const uint32_t oc = (C >> 2) & M2;  // odd sites: right neighbours, shifted: left ones
+        ctr = C & M2;
+        nbs = oc + ((oc << 4) | sv) + (U & M2) + (D & M2);
+    } else {
+        const uint32_t ec = C & M2;  // even sites: left neighbours, shifted: right ones
+        ctr = (C >> 2) & M2;
+        nbs = ec + ((ec >> 4) | (sv << (4 * (SLOTS - 1)))) + ((U >> 2) & M2) + ((D >> 2) & M2);
+    }
+
     uint32_t r1[SLOTS], r3[SLOTS];
 #pragma unroll
-    for (int g = 0; g < SLOTS / 4; ++g) {
-        const uint32_t cc = st.c0 + 1u + (uint32_t)g;
-        const uint4 a = philox<R>(cc, seed, iter, kCtrTag, k1);
-        const uint4 b = philox<R>(cc, seed, iter, kCtrTag, k3);
-        r1[4 * g + 0] = a.x; r1[4 * g + 1] = a.y; r1[4 * g + 2] = a.z; r1[4 * g + 3] = a.w;
-        r3[4 * g + 0] = b.x; r3[4 * g + 1] = b.y; r3[4 * g + 2] = b.z; r3[4 * g + 3] = b.w;
+    for (int t = 0; t < 4; ++t) {
+        r1[t] = Q.q0.r1[t];
+        r3[t] = Q.q0.r3[t];
+        if (SLOTS == 8) {
+            r1[t + 4] = Q.q1.r1[t];
+            r3[t + 4] = Q.q1.r3[t];
+        }
     }
-    st.c0 += (len + 3u) >> 2;
+    // the next window's random numbers: independent of everything below,
+    // so they fill the issue slots of the sequential scan
+    refill<R>(Q, SLOTS / 4, seed, iter, k1, k3);
 
-    // proposals of the whole window (independent of each other)
+    // proposals of the whole window (independent of each other):
+    // s -> s +/- 1 with the cyclic wrap is (code + 1 + d) mod 3 on s+1 codes
     int dE[SLOTS], dDel[SLOTS], dM[SLOTS];
-    uint32_t vold[SLOTS], vnew[SLOTS];
-    float lu[SLOTS];
+    WT f2[SLOTS];
+    float lf[SLOTS];
+    uint32_t vnib = 0;
 #pragma unroll
     for (int t = 0; t < SLOTS; ++t) {
-        constexpr int dummy = 0;
-        (void)dummy;
-        const int pos = 2 * t + HALF;  // site offset inside the word
-        const uint32_t vo = (C >> (2 * pos)) & 3u;
-        uint32_t vl, vr;
-        if (HALF == 0) {
-            vl = (t == 0) ? sv : ((C >> (2 * pos - 2)) & 3u);
-            vr = (C >> (2 * pos + 2)) & 3u;
-        } else {
-            vl = (C >> (2 * pos - 2)) & 3u;
-            vr = (t == SLOTS - 1) ? sv : ((C >> ((2 * pos + 2) & 31)) & 3u);
-        }
-        const int nb = (int)(vl + vr + ((U >> (2 * pos)) & 3u) + ((D >> (2 * pos)) & 3u)) - 4;
-        const int so = (int)vo - 1;
-        int sn = so + ((r3[t] >> 31) ? -1 : 1);  // u01f(r3) < 0.5  <=>  r3 < 2^31
-        sn = (sn == 2) ? -1 : ((sn == -2) ? 1 : sn);
-        dE[t] = -(sn - so) * nb;
-        dDel[t] = sn * sn - so * so;
-        dM[t] = sn - so;
-        vold[t] = vo;
-        vnew[t] = (uint32_t)(sn + 1);
-        lu[t] = logf(u01f(r1[t]));
+        const uint32_t vo = (ctr >> (4 * t)) & 3u;
+        const int nbc = (int)((nbs >> (4 * t)) & 15u);
+        const uint32_t x = vo + 1u + (r3[t] >> 31);  // u01f(r3) < 0.5  <=>  r3 < 2^31
+        const uint32_t vn = x >= 3u ? x - 3u : x;
+        const int dv = (int)vn - (int)vo;
+        dE[t] = dv * (4 - nbc);  // -(s_new - s_old) * sum of neighbour spins
+        dDel[t] = (int)(vn != 1u) - (int)(vo != 1u);
+        dM[t] = dv;
+        f2[t] = (WT)(-2 * dE[t]);
+        lf[t] = __logf(u01f(r1[t]));
+        vnib |= vn << (4 * t);
     }
 
-    // sequential accept/reject over E_Delta
-    WT wE = wS[st.E];
-    uint32_t Cn = C;
+    // sequential accept/reject over E_Delta:
+    //   accept  <=>  diff >= 0  ||  logf(u) < diff,
+    //   diff = (float)(-2 dE) + w[E + dDel] - w[E]   (muca_delta_multigpu.cu:810-816)
+    // decided with __logf(u) unless it lies within eps of diff in some lane;
+    // then the window is replayed with the exact logf(u).
+    const ChainState s0 = st;
+    const WT wE0 = wS[st.E];
+    WT wE = wE0;
+    uint32_t accm = 0;
+    bool near = false;
     int Es[SLOTS], Ms[SLOTS];
 #pragma unroll
     for (int t = 0; t < SLOTS; ++t) {
-        const int pos = 2 * t + HALF;
         const WT wn = wS[st.E + dDel[t]];
         WT diff;
         if (MODE == kModeWeight)
-            diff = __fsub_rn(__fadd_rn((float)(-2 * dE[t]), (float)wn), (float)wE);
+            diff = __fsub_rn(__fadd_rn((float)f2[t], (float)wn), (float)wE);
         else
-            diff = __dsub_rn(__dadd_rn((double)(-2 * dE[t]), (double)wn), (double)wE);
-        const bool acc = ((uint32_t)t < len) && ((diff >= (WT)0) || ((WT)lu[t] < diff));
-        st.E += acc ? dDel[t] : 0;
-        st.EJ += acc ? dE[t] : 0;
-        if (MODE == kModeProduce) st.M += acc ? dM[t] : 0;
-        wE = acc ? wn : wE;
-        const uint32_t v = acc ? vnew[t] : vold[t];
-        Cn = (Cn & ~(3u << (2 * pos))) | (v << (2 * pos));
+            diff = __dsub_rn(__dadd_rn((double)f2[t], (double)wn), (double)wE);
+        const WT l = (WT)lf[t];
+        const bool acc = (diff >= (WT)0) || (l < diff);
+        near |= (diff < (WT)0) && (fabs(l - diff) <= eps);
+        if (acc) {
+            st.E += dDel[t];
+            st.EJ += dE[t];
+            st.M += dM[t];
+            wE = wn;
+            accm |= 0xFu << (4 * t);
+        }
         Es[t] = st.E;
         Ms[t] = st.M;
     }
-    *pc = Cn;
+    if (__any_sync(0xffffffffu, near)) {
+        st = s0;
+        wE = wE0;
+        accm = 0;
+#pragma unroll
+        for (int t = 0; t < SLOTS; ++t) {
+            const WT wn = wS[st.E + dDel[t]];
+            WT diff;
+            if (MODE == kModeWeight)
+                diff = __fsub_rn(__fadd_rn((float)f2[t], (float)wn), (float)wE);
+            else
+                diff = __dsub_rn(__dadd_rn((double)f2[t], (double)wn), (double)wE);
+            bool acc = diff >= (WT)0;
+            if (!acc) acc = (WT)logf(u01f(r1[t])) < diff;
+            if (acc) {
+                st.E += dDel[t];
+                st.EJ += dE[t];
+                st.M += dM[t];
+                wE = wn;
+                accm |= 0xFu << (4 * t);
+            }
+            Es[t] = st.E;
+            Ms[t] = st.M;
+        }
+    }
+    const uint32_t merged = (ctr & ~accm) | (vnib & accm);
+    *pc = (HALF == 0) ? ((C & ~M2) | merged) : ((C & M2) | (merged << 2));
     if (rec) {
 #pragma unroll
         for (int t = 0; t < SLOTS; ++t) {
-            if ((uint32_t)t < len) {
-                if (MODE == kModeWeight)
-                    atomicAdd(&histS[Es[t]], 1u);
-                else
-                    atomicAdd(&histG[(uint32_t)(Ms[t] + Es[t] * Es[t] + 2 * Es[t]) >> 1], 1ull);
-            }
+            if (MODE == kModeWeight)
+                atomicAdd(&histS[Es[t]], 1u);
+            else
+                atomicAdd(&histG[(uint32_t)(Ms[t] + Es[t] * Es[t] + 2 * Es[t]) >> 1], 1ull);
         }
     }
+}
+
+// The first `len` (< cnt) attempts of a window, one at a time as the
+// reference writes them; only the last window of a phase can be partial.
+template <int MODE, int R>
+__device__ __noinline__ void partial_window(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
+                                            uint32_t row, uint32_t q, uint32_t half, uint32_t len, bool rec,
+                                            const typename WeightType<MODE>::T *__restrict__ wS,
+                                            uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
+                                            ChainState &st, Queue &Q, uint32_t seed, uint32_t iter,
+                                            const RoundKeys<R> &k1, const RoundKeys<R> &k3)
+{
+    using WT = typename WeightType<MODE>::T;
+    auto word = [&](uint32_t r, uint32_t c) -> uint32_t * { return lat + (size_t)(r * WPR + (c >> 4)) * cpb; };
+    auto get = [&](uint32_t r, uint32_t c) -> int { return (int)spin_code(*word(r, c), c) - 1; };
+    const uint32_t rup = (row + 1 == L) ? 0u : row + 1;
+    const uint32_t rdn = (row == 0) ? L - 1 : row - 1;
+    for (uint32_t t = 0; t < len; ++t) {
+        const uint32_t r1 = t < 4 ? Q.q0.r1[t & 3] : Q.q1.r1[t & 3];
+        const uint32_t r3 = t < 4 ? Q.q0.r3[t & 3] : Q.q1.r3[t & 3];
+        const uint32_t col = 16u * q + 2u * t + half;
+        const uint32_t cl = col ? col - 1 : L - 1, cr = (col + 1 == L) ? 0u : col + 1;
+        const int os = get(row, col);
+        int ns = os + ((r3 >> 31) ? -1 : 1);
+        ns = ns - 3 * (ns == 2) + 3 * (ns == -2);
+        const int nb = get(row, cl) + get(row, cr) + get(rup, col) + get(rdn, col);
+        const int dE = -(ns - os) * nb, dDel = ns * ns - os * os, dM = ns - os;
+        WT diff;
+        if (MODE == kModeWeight)
+            diff = __fsub_rn(__fadd_rn((float)(-2 * dE), (float)wS[st.E + dDel]), (float)wS[st.E]);
+        else
+            diff = __dsub_rn(__dadd_rn((double)(-2 * dE), (double)wS[st.E + dDel]), (double)wS[st.E]);
+        bool acc = diff >= (WT)0;
+        if (!acc) acc = (WT)logf(u01f(r1)) < diff;
+        if (acc) {
+            uint32_t *p = word(row, col);
+            const uint32_t sh = 2u * (col & 15u);
+            *p = (*p & ~(3u << sh)) | ((uint32_t)(ns + 1) << sh);
+            st.E += dDel;
+            st.EJ += dE;
+            st.M += dM;
+        }
+        if (rec) {
+            if (MODE == kModeWeight)
+                atomicAdd(&histS[st.E], 1u);
+            else
+                atomicAdd(&histG[(uint32_t)(st.M + st.E * st.E + 2 * st.E) >> 1], 1ull);
+        }
+    }
+    refill<R>(Q, (len + 3u) >> 2, seed, iter, k1, k3);
 }
 
 template <int MODE>
@@ -203,7 +344,7 @@ __device__ __forceinline__ uint32_t *prologue(const SweepArgs &a, unsigned char 
 }
 
 template <int MODE, int R, bool LAT_SMEM>
-__global__ void __launch_bounds__(256) k_sweep_fast(const SweepArgs a)
+__global__ void __launch_bounds__(256, 1) k_sweep_fast(const SweepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     using WT = typename WeightType<MODE>::T;
@@ -232,7 +373,11 @@ __global__ void __launch_bounds__(256) k_sweep_fast(const SweepArgs a)
     st.E = active ? a.edel[chain] : 0;
     st.EJ = active ? a.ej[chain] : 0;
     st.M = (active && MODE == kModeProduce) ? a.mag[chain] : 0;
-    st.c0 = 0;
+    Queue Q;
+    Q.q0 = gen_group<R>(1u, seed, iter, k1, k3);
+    Q.q1 = gen_group<R>(2u, seed, iter, k1, k3);
+    Q.qc = 2u;
+    const WT eps = (WT)a.log_eps;
     const uint32_t L = a.L, WPR = a.WPR;
     // a block's u32 histogram bins can take at most 2^31 counts between flushes
     const unsigned long long flush_every = (MODE == kModeWeight) ? (0x80000000ull / cpb) : ~0ull;
@@ -245,22 +390,25 @@ __global__ void __launch_bounds__(256) k_sweep_fast(const SweepArgs a)
         uint32_t row = 0, q = 0, half = 0;
         while (i < n) {
             const uint32_t cnt = (min(16u * q + 16u, L) - 16u * q) >> 1;
-            const unsigned long long rem = n - i;
-            const uint32_t len = rem < cnt ? (uint32_t)rem : cnt;
-            if (cnt == 8) {
-                if (half) window<MODE, R, 8, 1>(lat, cpb, L, WPR, row, q, len, rec_lane, wS, histS, a.hist, st, seed, iter, k1, k3);
-                else      window<MODE, R, 8, 0>(lat, cpb, L, WPR, row, q, len, rec_lane, wS, histS, a.hist, st, seed, iter, k1, k3);
-            } else {
-                if (half) window<MODE, R, 4, 1>(lat, cpb, L, WPR, row, q, len, rec_lane, wS, histS, a.hist, st, seed, iter, k1, k3);
-                else      window<MODE, R, 4, 0>(lat, cpb, L, WPR, row, q, len, rec_lane, wS, histS, a.hist, st, seed, iter, k1, k3);
+            if (n - i < cnt) {
+                partial_window<MODE, R>(lat, cpb, L, WPR, row, q, half, (uint32_t)(n - i), rec_lane, wS, histS,
+                                        a.hist, st, Q, seed, iter, k1, k3);
+                break;
             }
-            i += len;
+            if (cnt == 8) {
+                if (half) window<MODE, R, 8, 1>(lat, cpb, L, WPR, row, q, rec_lane, wS, histS, a.hist, st, Q, seed, iter, k1, k3, eps);
+                else      window<MODE, R, 8, 0>(lat, cpb, L, WPR, row, q, rec_lane, wS, histS, a.hist, st, Q, seed, iter, k1, k3, eps);
+            } else {
+                if (half) window<MODE, R, 4, 1>(lat, cpb, L, WPR, row, q, rec_lane, wS, histS, a.hist, st, Q, seed, iter, k1, k3, eps);
+                else      window<MODE, R, 4, 0>(lat, cpb, L, WPR, row, q, rec_lane, wS, histS, a.hist, st, Q, seed, iter, k1, k3, eps);
+            }
+            i += cnt;
             if (++q == WPR) {
                 q = 0;
                 if (++row == L) { row = 0; half ^= 1u; }
             }
             if (rec) {
-                since_flush += len;
+                since_flush += cnt;
                 if (since_flush >= flush_every && i < n) {
                     flush_hist<MODE>(histS, a.hist, a.N);
                     since_flush = 0;
@@ -281,8 +429,6 @@ __global__ void __launch_bounds__(256) k_sweep_fast(const SweepArgs a)
     flush_hist<MODE>(histS, a.hist, a.N);
 }
 
-// Generic kernel: the reference step as written, for any L, on the packed
-// layout; sweep order and neighbours from the reference tables.
 template <int MODE, int R, bool LAT_SMEM>
 __global__ void __launch_bounds__(256) k_sweep_generic(const SweepArgs a)
 {
@@ -389,6 +535,40 @@ __global__ void __launch_bounds__(256) k_sweep_generic(const SweepArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// Worst-case |__logf(u) - logf(u)| over every value u01fixedpt<float> can
+// return (u = (2k+1) 2^-24, k < 2^23), as the bits of a non-negative float.
+__global__ void k_logf_bracket(unsigned int *maxbits)
+{
+    unsigned int m = 0;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < (1u << 23); k += gridDim.x * blockDim.x) {
+        const float u = u01f(k << 9);
+        const float e = fabsf(__logf(u) - logf(u));
+        m = max(m, __float_as_uint(e));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxbits, m);
+}
+
+cudaError_t measure_logf_bracket(float *max_abs_err, cudaStream_t s)
+{
+    unsigned int *d = nullptr, h = 0;
+    cudaError_t e = cudaMalloc(&d, sizeof(unsigned int));
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(d, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) {
+        k_logf_bracket<<<152 * 8, 256, 0, s>>>(d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof h, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d);
+    float f;
+    std::memcpy(&f, &h, sizeof f);
+    *max_abs_err = f;
+    return e;
+}
+
 SweepPlan plan_sweep(int mode, int rounds, uint32_t L, uint32_t nchains, size_t smem_optin, int sms)
 {
     SweepPlan p{};

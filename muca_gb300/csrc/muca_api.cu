@@ -44,6 +44,7 @@ struct muca_ctx {
     int8_t *d_tmp = nullptr;
     unsigned long long *d_bad = nullptr, *h_bad = nullptr;
     uint64_t device_bytes = 0;
+    double log_eps = 0;
     std::string err;
 };
 
@@ -151,6 +152,7 @@ SweepArgs sweep_args(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint32_t se
         a.k1_mul = 1; a.k1_add = 0; a.k1_hi = 0xdecafbadu;
         a.k3_mul = 1; a.k3_add = 40000; a.k3_hi = 0xdecafeadu;
     }
+    a.log_eps = c->log_eps;
     a.dyn = nullptr;
     return a;
 }
@@ -259,6 +261,20 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
         CREATE_TRY(cudaMemcpyAsync(c->d_index, ix.data(), ix.size() * 4, cudaMemcpyHostToDevice, c->stream));
         CREATE_TRY(cudaMemcpyAsync(c->d_naver, nv.data(), nv.size() * 4, cudaMemcpyHostToDevice, c->stream));
     }
+    {
+        // the bound of the fast acceptance test, measured once per device
+        static float maxerr_dev[64];
+        static bool have[64];
+        if (c->device < 0 || c->device >= 64) { fail(c, MUCA_ERR_BAD_ARG, "device %d", c->device); return bail(MUCA_ERR_BAD_ARG); }
+        if (!have[c->device]) {
+            CREATE_TRY(measure_logf_bracket(&maxerr_dev[c->device], c->stream));
+            have[c->device] = true;
+        }
+        const float m = maxerr_dev[c->device];
+        // a finite bound enables the fast test (twice the worst case);
+        // anything else keeps every decision on the exact logf
+        c->log_eps = (m >= 0.0f && m < 1e-2f) ? 2.0 * (double)m + 1e-30 : 1e30;
+    }
     CREATE_TRY(cudaStreamSynchronize(c->stream));
 #undef CREATE_TRY
     *out = c;
@@ -289,6 +305,7 @@ muca_status muca_get_info(const muca_ctx *c, muca_info *o)
     o->smem_bytes = (uint32_t)c->plan.smem;
     o->sms = (uint32_t)c->sms;
     o->device_bytes = c->device_bytes;
+    o->log_bracket = c->log_eps;
     return MUCA_OK;
 }
 

@@ -24,6 +24,9 @@ struct SweepArgs {
     uint32_t seed_base, seed_dev_mul, iter;
     unsigned long long therm, nup;
     uint32_t k1_mul, k1_add, k1_hi, k3_mul, k3_add, k3_hi;
+    // bound on |__logf(u) - logf(u)| over all u01fixedpt<float> values
+    // (measure_logf_bracket) times a safety factor; 0 disables the fast test
+    double log_eps;
     // optional device-resident (iter, nup, skip) for graph-captured loops;
     // when non-null they override iter/nup and a nonzero skip makes the
     // launch a no-op.
@@ -45,6 +48,8 @@ struct SweepPlan {
 // Chooses placement and block shape for (mode, L, nchains) on a device with
 // `smem_optin` bytes of opt-in shared memory per block and `sms` SMs.
 SweepPlan plan_sweep(int mode, int rounds, uint32_t L, uint32_t nchains, size_t smem_optin, int sms);
+// Worst case of |__logf(u) - logf(u)| over u = (2k+1) 2^-24, k < 2^23 (exhaustive, on the device).
+cudaError_t measure_logf_bracket(float *max_abs_err, cudaStream_t s);
 cudaError_t launch_sweep(const SweepPlan &p, const SweepArgs &a, cudaStream_t s);
 
 // Lattice helpers (k_lattice.cu).
