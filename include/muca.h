@@ -81,6 +81,8 @@ typedef struct muca_params {
     uint32_t dev_offset; /* index of the first emulated device (a process that runs
                             reference devices k..k+ndev-1 sets k; seeds and init
                             counters follow the device index) */
+    uint32_t kernel;     /* sweep kernel: 0 auto, 1 generic (reference step by step),
+                            2 windowed, 3 warp-specialised (2 and 3 need L % 8 == 0) */
 } muca_params;
 
 typedef struct muca_info {
@@ -89,6 +91,8 @@ typedef struct muca_info {
     uint64_t device_bytes;
     double log_bracket;  /* bound used by the fast acceptance test: twice the measured
                             max |__logf(u) - logf(u)| over all u01fixedpt<float> values */
+    uint32_t kernel;      /* sweep kernel in use (see muca_params.kernel) */
+    uint32_t threads_per_block;
 } muca_info;
 
 /* Histogram summary (muca_delta_multigpu.cu:431-447 and the min/mean test of

@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libmuca.so")
 MODE_WEIGHT, MODE_PRODUCE = 0, 1
 INIT_WEIGHT, INIT_PRODUCE, INIT_BASELINE, INIT_ORDERED = 0, 1, 2, 3
 UPDATE_TRIVIAL, UPDATE_TRIVIAL_CPU, UPDATE_RECURSION = 0, 1, 2
+KERNEL_AUTO, KERNEL_GENERIC, KERNEL_WINDOWED, KERNEL_SPECIALIZED = 0, 1, 2, 3
 STATUS = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "TIMEOUT", 4: "NOT_CONVERGED", 5: "IO", 6: "STATE"}
 
 # Every symbol include/muca.h declares (the C-ABI surface).
@@ -44,14 +45,16 @@ class MucaError(RuntimeError):
 
 class Params(C.Structure):
     _fields_ = [("L", C.c_uint32), ("nchains", C.c_uint32), ("ndev", C.c_uint32), ("device", C.c_int32),
-                ("rounds", C.c_uint32), ("mode", C.c_uint32), ("stream", C.c_void_p), ("dev_offset", C.c_uint32)]
+                ("rounds", C.c_uint32), ("mode", C.c_uint32), ("stream", C.c_void_p), ("dev_offset", C.c_uint32),
+                ("kernel", C.c_uint32)]
 
 
 class Info(C.Structure):
     _fields_ = [("L", C.c_uint32), ("N", C.c_uint32), ("nchains_total", C.c_uint32),
                 ("chains_per_block", C.c_uint32), ("blocks", C.c_uint32), ("lattice_in_smem", C.c_uint32),
                 ("hist_in_smem", C.c_uint32), ("smem_bytes", C.c_uint32), ("sms", C.c_uint32),
-                ("weights_in_smem", C.c_uint32), ("device_bytes", C.c_uint64), ("log_bracket", C.c_double)]
+                ("weights_in_smem", C.c_uint32), ("device_bytes", C.c_uint64), ("log_bracket", C.c_double),
+                ("kernel", C.c_uint32), ("threads_per_block", C.c_uint32)]
 
 
 class HistStats(C.Structure):
@@ -149,10 +152,11 @@ def default_chains(device: int = 0) -> int:
 class Engine:
     """One simulation context (all chains of one lattice size) on one GPU."""
 
-    def __init__(self, L, nchains=0, ndev=1, mode=MODE_WEIGHT, rounds=7, device=0, stream=None, dev_offset=0):
+    def __init__(self, L, nchains=0, ndev=1, mode=MODE_WEIGHT, rounds=7, device=0, stream=None, dev_offset=0,
+                 kernel=KERNEL_AUTO):
         self._lib = lib()
         p = Params(L=L, nchains=nchains, ndev=ndev, device=device, rounds=rounds, mode=mode,
-                   stream=C.c_void_p(stream) if stream else None, dev_offset=dev_offset)
+                   stream=C.c_void_p(stream) if stream else None, dev_offset=dev_offset, kernel=kernel)
         h = C.c_void_p()
         st = self._lib.muca_create(C.byref(p), C.byref(h))
         if st:

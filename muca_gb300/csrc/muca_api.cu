@@ -43,6 +43,7 @@ struct muca_ctx {
     size_t jk_cap = 0;
     int8_t *d_tmp = nullptr;
     unsigned long long *d_bad = nullptr, *h_bad = nullptr;
+    unsigned int *d_err = nullptr, *h_err = nullptr;
     uint64_t device_bytes = 0;
     double log_eps = 0;
     std::string err;
@@ -81,10 +82,10 @@ void free_all(muca_ctx *c)
 {
     void *dp[] = {c->d_lat, c->d_ej, c->d_edel, c->d_mag, c->d_lnw, c->d_pacc, c->d_w32, c->d_hist,
                   c->d_index, c->d_naver, c->d_stats, c->d_ctl, c->d_recs, c->d_obs_part, c->d_obs_out,
-                  c->d_jk, c->d_tmp, c->d_bad};
+                  c->d_jk, c->d_tmp, c->d_bad, c->d_err};
     for (void *p : dp)
         if (p) cudaFree(p);
-    void *hp[] = {c->h_stats, c->h_ctl, c->h_obs_out, c->h_bad};
+    void *hp[] = {c->h_stats, c->h_ctl, c->h_obs_out, c->h_bad, c->h_err};
     for (void *p : hp)
         if (p) cudaFreeHost(p);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -121,6 +122,18 @@ muca_status recompute_energies(muca_ctx *c)
     return MUCA_OK;
 }
 
+muca_status check_err(muca_ctx *c)
+{
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_err, c->d_err, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (*c->h_err) {
+        const unsigned int e = *c->h_err;
+        cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream);
+        return fail(c, MUCA_ERR_TIMEOUT, "a bounded device wait gave up (error word 0x%x); results are invalid", e);
+    }
+    return MUCA_OK;
+}
+
 SweepArgs sweep_args(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint32_t seed_dev_mul, uint64_t therm,
                      uint64_t nup)
 {
@@ -153,6 +166,7 @@ SweepArgs sweep_args(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint32_t se
         a.k3_mul = 1; a.k3_add = 40000; a.k3_hi = 0xdecafeadu;
     }
     a.log_eps = c->log_eps;
+    a.err = c->d_err;
     a.dyn = nullptr;
     return a;
 }
@@ -215,7 +229,16 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
         return bail(MUCA_ERR_BAD_ARG);
     }
     c->nchains = (uint32_t)total;
-    c->plan = plan_sweep((int)c->mode, (int)rounds, c->L, c->nchains, c->smem_optin, c->sms);
+    if (p->kernel > 3) {
+        fail(c, MUCA_ERR_BAD_ARG, "kernel=%u (0..3)", p->kernel);
+        return bail(MUCA_ERR_BAD_ARG);
+    }
+    if ((p->kernel == 2 || p->kernel == 3) && !(p->L % 8 == 0 && p->L >= 8)) {
+        fail(c, MUCA_ERR_BAD_ARG, "kernel %u needs L %% 8 == 0", p->kernel);
+        return bail(MUCA_ERR_BAD_ARG);
+    }
+    const int want_kernel = p->kernel == 0 ? -1 : (int)p->kernel - 1;
+    c->plan = plan_sweep((int)c->mode, (int)rounds, c->L, c->nchains, c->smem_optin, c->sms, want_kernel);
     if (c->plan.smem > c->smem_optin) {
         fail(c, MUCA_ERR_BAD_ARG, "L=%u needs %zu B of shared memory per block (device has %zu)", c->L, c->plan.smem,
              c->smem_optin);
@@ -241,6 +264,9 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
     CREATE_TRY(dmalloc(c, &c->d_stats, 1));
     CREATE_TRY(dmalloc(c, &c->d_ctl, 1));
     CREATE_TRY(dmalloc(c, &c->d_bad, 1));
+    CREATE_TRY(dmalloc(c, &c->d_err, 1));
+    CREATE_TRY(cudaMallocHost((void **)&c->h_err, sizeof(unsigned int)));
+    CREATE_TRY(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream));
     CREATE_TRY(cudaMallocHost((void **)&c->h_stats, sizeof(HistStatsDev)));
     CREATE_TRY(cudaMallocHost((void **)&c->h_ctl, sizeof(RunCtl)));
     CREATE_TRY(cudaMallocHost((void **)&c->h_bad, sizeof(unsigned long long)));
@@ -253,7 +279,7 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
     CREATE_TRY(cudaMemsetAsync(c->d_pacc, 0, ((size_t)N + 1) * 8, c->stream));
     CREATE_TRY(cudaMemsetAsync(c->d_w32, 0, ((size_t)N + 1) * 4, c->stream));
     CREATE_TRY(cudaMemsetAsync(c->d_hist, 0, c->hist_len * 8, c->stream));
-    if (!c->plan.fast) {
+    if (c->plan.kernel == kKernelGeneric) {  // its sweep order and neighbours come from tables
         std::vector<uint32_t> nv, ix;
         build_tables(c->L, nv, ix);
         CREATE_TRY(dmalloc(c, &c->d_index, ix.size()));
@@ -306,6 +332,8 @@ muca_status muca_get_info(const muca_ctx *c, muca_info *o)
     o->sms = (uint32_t)c->sms;
     o->device_bytes = c->device_bytes;
     o->log_bracket = c->log_eps;
+    o->kernel = (uint32_t)c->plan.kernel + 1;
+    o->threads_per_block = c->plan.threads;
     return MUCA_OK;
 }
 
@@ -366,8 +394,7 @@ muca_status muca_get_lattice(muca_ctx *c, int8_t *lat, size_t n)
     if (muca_status st = ensure_tmp(c)) return st;
     CUDA_TRY(c, launch_unpack(c->d_lat, c->d_tmp, c->L, c->WPR, c->plan.cpb, c->nchains, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(lat, c->d_tmp, n, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    return MUCA_OK;
+    return check_err(c);
 }
 
 muca_status muca_get_chain_state(muca_ctx *c, int32_t *ej, int32_t *edel, int32_t *mag, size_t n)
@@ -378,8 +405,7 @@ muca_status muca_get_chain_state(muca_ctx *c, int32_t *ej, int32_t *edel, int32_
     if (ej) CUDA_TRY(c, cudaMemcpyAsync(ej, c->d_ej, n * 4, cudaMemcpyDeviceToHost, c->stream));
     if (edel) CUDA_TRY(c, cudaMemcpyAsync(edel, c->d_edel, n * 4, cudaMemcpyDeviceToHost, c->stream));
     if (mag) CUDA_TRY(c, cudaMemcpyAsync(mag, c->d_mag, n * 4, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    return MUCA_OK;
+    return check_err(c);
 }
 
 muca_status muca_set_weights(muca_ctx *c, const double *lnw, size_t n)
@@ -442,8 +468,7 @@ muca_status muca_get_histogram(muca_ctx *c, uint64_t *h, size_t n)
     if (n != c->hist_len) return fail(c, MUCA_ERR_BAD_ARG, "n=%zu, expected %zu", n, c->hist_len);
     CUDA_TRY(c, cudaSetDevice(c->device));
     CUDA_TRY(c, cudaMemcpyAsync(h, c->d_hist, n * 8, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    return MUCA_OK;
+    return check_err(c);
 }
 
 muca_status muca_set_histogram(muca_ctx *c, const uint64_t *h, size_t n)
@@ -476,7 +501,7 @@ static muca_status update_impl(muca_ctx *c, int rule, muca_hist_stats *st)
     CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, rule, c->d_stats, c->stream));
     if (!st) return MUCA_OK;  // enqueue only
     CUDA_TRY(c, cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(HistStatsDev), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (muca_status e = check_err(c)) return e;
     stats_out(*c->h_stats, st);
     return MUCA_OK;
 }
@@ -572,6 +597,7 @@ muca_status muca_weight_run(muca_ctx *c, const muca_run_opts *o, muca_run_result
     cudaEventDestroy(m0);
     cudaEventDestroy(m1);
     if (rs != MUCA_OK) return rs;
+    if (muca_status e = check_err(c)) return e;
     if (recs && cap) {
         std::vector<IterRecordDev> r(std::min<size_t>(cap, k_done));
         CUDA_TRY(c, cudaMemcpy(r.data(), c->d_recs, r.size() * sizeof(IterRecordDev), cudaMemcpyDeviceToHost));

@@ -31,23 +31,31 @@ struct SweepArgs {
     // when non-null they override iter/nup and a nonzero skip makes the
     // launch a no-op.
     const uint32_t *dyn;
+    // error word: bit 0 is set when a bounded wait inside a kernel gave up
+    unsigned int *err;
 };
 
 enum SweepMode { kModeWeight = 0, kModeProduce = 1 };
 
+enum SweepKernel { kKernelGeneric = 0, kKernelWindowed = 1, kKernelSpecialized = 2 };
+
 struct SweepPlan {
     int mode;
     int rounds;
-    bool fast;       // windowed kernel (L % 8 == 0) vs generic per-step kernel
+    int kernel;      // SweepKernel
+    bool fast;       // windowed kernels usable (L % 8 == 0)
     bool lat_smem;   // lattice resident in shared memory
-    uint32_t cpb;    // chains (threads) per block
+    uint32_t cpb;    // chains per block (lane stride of the packed lattice)
+    uint32_t threads;  // threads per block
     uint32_t blocks;
     size_t smem;     // dynamic shared memory bytes
 };
+constexpr uint32_t kRingDepth = 4;  // windows the producer warps may run ahead
 
 // Chooses placement and block shape for (mode, L, nchains) on a device with
 // `smem_optin` bytes of opt-in shared memory per block and `sms` SMs.
-SweepPlan plan_sweep(int mode, int rounds, uint32_t L, uint32_t nchains, size_t smem_optin, int sms);
+// kernel: -1 = choose (windowed when L % 8 == 0, else generic), else a SweepKernel.
+SweepPlan plan_sweep(int mode, int rounds, uint32_t L, uint32_t nchains, size_t smem_optin, int sms, int kernel = -1);
 // Worst case of |__logf(u) - logf(u)| over u = (2k+1) 2^-24, k < 2^23 (exhaustive, on the device).
 cudaError_t measure_logf_bracket(float *max_abs_err, cudaStream_t s);
 cudaError_t launch_sweep(const SweepPlan &p, const SweepArgs &a, cudaStream_t s);

@@ -40,6 +40,16 @@ def _ej_ed_copy(a):
     return np.ascontiguousarray(a, np.int32).copy()
 
 
+def _kernels(L):
+    """sweep kernels applicable to L: generic always, windowed and
+    warp-specialised when L % 8 == 0"""
+    return [1, 2, 3] if (L % 8 == 0 and L >= 8) else [1]
+
+
+def _with_kernels(cases):
+    return [c + (k,) for c in cases for k in _kernels(c[0])]
+
+
 @pytest.mark.parametrize("L,cpd,ndev,jack", [(4, 256, 1, 0), (6, 100, 2, 1), (8, 256, 1, 3), (16, 300, 2, 0),
                                              (72, 64, 1, 2), (10, 33, 3, 0)])
 def test_init_weight_scheme(muca, orc, L, cpd, ndev, jack):
@@ -91,13 +101,14 @@ SWEEPS = [
 ]
 
 
-@pytest.mark.parametrize("L,cpd,ndev,therm,nup", SWEEPS)
-def test_weight_sweep_vs_oracle(muca, orc, L, cpd, ndev, therm, nup):
+@pytest.mark.parametrize("L,cpd,ndev,therm,nup,kernel", _with_kernels(SWEEPS))
+def test_weight_sweep_vs_oracle(muca, orc, L, cpd, ndev, therm, nup, kernel):
     rng = np.random.default_rng(L * 1000 + nup)
     N = L * L
     lnw = _weights(N, rng)
     it = int(rng.integers(0, 50))
-    with muca.Engine(L, nchains=cpd, ndev=ndev) as e:
+    with muca.Engine(L, nchains=cpd, ndev=ndev, kernel=kernel) as e:
+        assert e.info.kernel == kernel
         e.set_weights(lnw)
         e.init_chains(muca.INIT_WEIGHT, 1)
         lat0 = e.get_lattice()
@@ -115,9 +126,10 @@ def test_weight_sweep_vs_oracle(muca, orc, L, cpd, ndev, therm, nup):
     assert int(h.sum()) == cpd * ndev * nup
 
 
-@pytest.mark.parametrize("L,therm,nup", [(8, 64, 500), (16, 256, 300), (24, 576, 100), (72, 5184, 41),
-                                         (4, 16, 200), (6, 36, 99), (10, 100, 57)])
-def test_weight_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup):
+@pytest.mark.parametrize("L,therm,nup,kernel", _with_kernels([(8, 64, 500), (16, 256, 300), (24, 576, 100),
+                                                                (72, 5184, 41), (4, 16, 200), (6, 36, 99),
+                                                                (10, 100, 57)]))
+def test_weight_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup, kernel):
     if refgpu is None:
         pytest.skip("reference cubins not present in this checkout")
     rng = np.random.default_rng(L + 7)
@@ -125,7 +137,7 @@ def test_weight_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup):
     lnw = _weights(N, rng)
     w32 = lnw.astype(np.float32)
     it = 3
-    with muca.Engine(L, nchains=256) as e:
+    with muca.Engine(L, nchains=256, kernel=kernel) as e:
         e.set_weights(lnw)
         e.init_chains(muca.INIT_WEIGHT, 0)
         lat0 = e.get_lattice()
@@ -157,11 +169,12 @@ def test_reference_kernel_init_energies(muca, orc, refgpu):
 
 
 @pytest.mark.parametrize("rounds", [7, 10])
-def test_weight_sweep_rounds(muca, orc, rounds):
+@pytest.mark.parametrize("kernel", [1, 2, 3])
+def test_weight_sweep_rounds(muca, orc, rounds, kernel):
     L, cpd = 16, 96
     rng = np.random.default_rng(rounds)
     lnw = _weights(L * L, rng)
-    with muca.Engine(L, nchains=cpd, rounds=rounds) as e:
+    with muca.Engine(L, nchains=cpd, rounds=rounds, kernel=kernel) as e:
         e.set_weights(lnw)
         e.init_chains(muca.INIT_WEIGHT, 0)
         lat0 = e.get_lattice()
@@ -175,13 +188,14 @@ def test_weight_sweep_rounds(muca, orc, rounds):
     np.testing.assert_array_equal(h, oh)
 
 
-@pytest.mark.parametrize("L,cpd,therm,nup", [(8, 256, 64, 300), (16, 200, 0, 1000), (4, 100, 16, 123),
-                                             (24, 64, 576, 50), (6, 64, 0, 200)])
-def test_produce_sweep_vs_oracle(muca, orc, L, cpd, therm, nup):
+@pytest.mark.parametrize("L,cpd,therm,nup,kernel", _with_kernels([(8, 256, 64, 300), (16, 200, 0, 1000),
+                                                                    (4, 100, 16, 123), (24, 64, 576, 50),
+                                                                    (6, 64, 0, 200), (72, 40, 5184, 1000)]))
+def test_produce_sweep_vs_oracle(muca, orc, L, cpd, therm, nup, kernel):
     rng = np.random.default_rng(L * 7 + nup)
     N = L * L
     lnw = _weights(N, rng)
-    with muca.Engine(L, nchains=cpd, mode=muca.MODE_PRODUCE) as e:
+    with muca.Engine(L, nchains=cpd, mode=muca.MODE_PRODUCE, kernel=kernel) as e:
         e.set_weights(lnw)
         e.init_chains(muca.INIT_PRODUCE, 0)
         lat0 = e.get_lattice()
@@ -200,14 +214,15 @@ def test_produce_sweep_vs_oracle(muca, orc, L, cpd, therm, nup):
     np.testing.assert_array_equal(h, oh)
 
 
-@pytest.mark.parametrize("L,therm,nup", [(8, 64, 300), (16, 256, 200), (4, 0, 150), (6, 36, 100)])
-def test_produce_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup):
+@pytest.mark.parametrize("L,therm,nup,kernel", _with_kernels([(8, 64, 300), (16, 256, 200), (4, 0, 150),
+                                                                (6, 36, 100)]))
+def test_produce_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup, kernel):
     if refgpu is None:
         pytest.skip("reference cubins not present in this checkout")
     rng = np.random.default_rng(L * 3 + 1)
     N = L * L
     lnw = _weights(N, rng)
-    with muca.Engine(L, nchains=256, mode=muca.MODE_PRODUCE) as e:
+    with muca.Engine(L, nchains=256, mode=muca.MODE_PRODUCE, kernel=kernel) as e:
         e.set_weights(lnw)
         e.init_chains(muca.INIT_PRODUCE, 0)
         lat0 = e.get_lattice()
@@ -369,7 +384,8 @@ def test_jackknife_vs_oracle(muca, orc):
 
 # ---- full-size workload (L=72, 16384 chains) -------------------------------------------------
 
-def test_full_size_L72_properties(muca, orc):
+@pytest.mark.parametrize("kernel", [2, 3])
+def test_full_size_L72_properties(muca, orc, kernel):
     """The benchmark workload: every chain's final E_Delta / E_J is
     consistent with its lattice, the histogram holds exactly chains*nup
     entries, and a subset of chains matches the oracle bit for bit."""
@@ -377,8 +393,8 @@ def test_full_size_L72_properties(muca, orc):
     N = L * L
     rng = np.random.default_rng(72)
     lnw = _weights(N, rng, sigma=0.8)
-    with muca.Engine(L, nchains=nch) as e:
-        assert e.info.lattice_in_smem == 1
+    with muca.Engine(L, nchains=nch, kernel=kernel) as e:
+        assert e.info.lattice_in_smem == 1 and e.info.kernel == kernel
         e.set_weights(lnw)
         e.init_chains(muca.INIT_WEIGHT, 0)
         lat0 = e.get_lattice()
