@@ -123,6 +123,8 @@ typedef struct muca_run_opts {
     uint32_t nup_schedule;  /* 0: reference ((NUP+1)*1.01 once width==N, :379-382); 1: doubling */
     double min_over_mean;   /* threshold for flat_minmean (0 = 0.5) */
     double d_kl_max;        /* threshold of the D_KL test (0 = 1e-4) */
+    uint32_t width_start;   /* initial running width (0 = 10, :314); the reference keeps the
+                               previous jack's width for jack > 0 */
 } muca_run_opts;
 
 typedef struct muca_iter_record {
@@ -201,11 +203,20 @@ muca_status muca_update_weights(muca_ctx *ctx, uint32_t rule, muca_hist_stats *s
  * recs (optional, capacity cap) receives one record per iteration. */
 muca_status muca_weight_run(muca_ctx *ctx, const muca_run_opts *opts, muca_run_result *res,
                             muca_iter_record *recs, size_t cap);
+/* Same, calling cb(record, user) on the host after every iteration (the
+ * per-iteration log line of :439). */
+typedef void (*muca_iter_callback)(const muca_iter_record *rec, void *user);
+muca_status muca_weight_run_stream(muca_ctx *ctx, const muca_run_opts *opts, muca_run_result *res,
+                                   muca_iter_callback cb, void *user);
 
 /* Production.  Shift lnW (produce2_multigpu.cu:391-400), form
  * boltz_j = exp(-beta*delta*j - lnW_j) (:297) and reweight the current 2D
- * histogram into observables (:498-518), all on the device in FP64. */
+ * histogram into observables (:498-518), all on the device in FP64.
+ * The shift applies to the reweighting copy of the weights only (set by
+ * muca_set_weights, shifted cumulatively as the reference shifts its host
+ * copy); the sweep keeps the weights as set, as the reference kernel does. */
 muca_status muca_weight_shift(muca_ctx *ctx, double beta, double delta);
+muca_status muca_get_reweighting_weights(muca_ctx *ctx, double *lnw, size_t n);
 muca_status muca_compute_observables(muca_ctx *ctx, double beta, double delta, muca_observables *out);
 /* Leave-one-out jackknife (muca_delta_multigpu.cu:620-635) on the device. */
 muca_status muca_jackknife(muca_ctx *ctx, const double *x, uint32_t n, double *avg, double *err);

@@ -33,7 +33,7 @@ EXPORTS = [
     "muca_set_weights", "muca_get_weights", "muca_sweep", "muca_sweep_accumulate",
     "muca_clear_histogram", "muca_get_histogram", "muca_set_histogram", "muca_histogram_stats", "muca_update_weights",
     "muca_weight_run", "muca_weight_shift", "muca_compute_observables", "muca_jackknife",
-    "muca_philox_peak",
+    "muca_philox_peak", "muca_weight_run_stream", "muca_get_reweighting_weights",
 ]
 
 
@@ -67,7 +67,7 @@ class RunOpts(C.Structure):
     _fields_ = [("jack", C.c_uint32), ("starting_M", C.c_uint32), ("therm", C.c_uint32), ("rule", C.c_uint32),
                 ("hold_until_full", C.c_uint32), ("flat_minmean", C.c_uint32), ("max_iter", C.c_uint32),
                 ("init_scheme", C.c_uint32), ("reinit_chains", C.c_uint32), ("nup_schedule", C.c_uint32),
-                ("min_over_mean", C.c_double), ("d_kl_max", C.c_double)]
+                ("min_over_mean", C.c_double), ("d_kl_max", C.c_double), ("width_start", C.c_uint32)]
 
 
 class IterRecord(C.Structure):
@@ -76,10 +76,16 @@ class IterRecord(C.Structure):
                 ("kernel_ms", C.c_double), ("memcpy_ms", C.c_double)]
 
 
+ITER_CB = None  # set below, after IterRecord
+
+
 class RunResult(C.Structure):
     _fields_ = [("iterations", C.c_uint32), ("converged", C.c_uint32), ("width_reached_iter", C.c_uint32),
                 ("total_run", C.c_uint64), ("nwidth_step", C.c_uint64), ("total_kernel_s", C.c_double),
                 ("total_mem_s", C.c_double), ("nwidth_time_s", C.c_double), ("wall_s", C.c_double)]
+
+
+ITER_CB = C.CFUNCTYPE(None, C.POINTER(IterRecord), C.c_void_p)
 
 
 class Observables(C.Structure):
@@ -125,6 +131,8 @@ def lib():
     L.muca_update_weights.argtypes = [vp, C.c_uint32, C.POINTER(HistStats)]
     L.muca_weight_run.argtypes = [vp, C.POINTER(RunOpts), C.POINTER(RunResult), C.POINTER(IterRecord), C.c_size_t]
     L.muca_weight_shift.argtypes = [vp, C.c_double, C.c_double]
+    L.muca_get_reweighting_weights.argtypes = [vp, f64, C.c_size_t]
+    L.muca_weight_run_stream.argtypes = [vp, C.POINTER(RunOpts), C.POINTER(RunResult), ITER_CB, C.c_void_p]
     L.muca_compute_observables.argtypes = [vp, C.c_double, C.c_double, C.POINTER(Observables)]
     L.muca_jackknife.argtypes = [vp, f64, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.muca_philox_peak.argtypes = [C.c_int32, C.c_uint32, C.POINTER(C.c_double)]
@@ -272,6 +280,11 @@ class Engine:
     # -- production --------------------------------------------------------
     def weight_shift(self, beta, delta):
         self._ck(self._lib.muca_weight_shift(self._h, beta, delta))
+
+    def reweighting_weights(self):
+        a = np.zeros(self.N + 1)
+        self._ck(self._lib.muca_get_reweighting_weights(self._h, a, a.size))
+        return a
 
     def observables(self, beta, delta):
         o = Observables()

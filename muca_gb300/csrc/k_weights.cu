@@ -114,8 +114,9 @@ __global__ void __launch_bounds__(kUpdThreads) k_weight_update(const unsigned lo
             if (wt > st.width) st.width = wt;
             if (st.width == N && !st.reach) { st.reach = 1; st.reach_k = st.k; st.nwidth_step = st.total_run; }
             const bool conv = ctl->flat_minmean ? (mom >= ctl->mom_thr) : (st.width == N && kl < ctl->dkl_max);
-            if (st.k < ctl->rec_cap && ctl->recs) {
-                IterRecordDev &r = ctl->recs[st.k];
+            const uint32_t ri = ctl->rec_ring ? (ctl->rec_cap ? st.k % ctl->rec_cap : 0u) : st.k;
+            if (ri < ctl->rec_cap && ctl->recs) {
+                IterRecordDev &r = ctl->recs[ri];
                 r.k = st.k; r.width_temp = wt; r.width = st.width; r.nupdates = st.nup;
                 r.total_run = st.total_run; r.d_kl = kl; r.min_over_mean = mom;
             }

@@ -30,7 +30,7 @@ struct muca_ctx {
     size_t lat_words = 0, hist_len = 0;
     uint32_t *d_lat = nullptr;
     int32_t *d_ej = nullptr, *d_edel = nullptr, *d_mag = nullptr;
-    double *d_lnw = nullptr, *d_pacc = nullptr;
+    double *d_lnw = nullptr, *d_pacc = nullptr, *d_lnw_obs = nullptr;
     float *d_w32 = nullptr;
     unsigned long long *d_hist = nullptr;
     uint32_t *d_index = nullptr, *d_naver = nullptr;
@@ -80,7 +80,7 @@ cudaError_t dmalloc(muca_ctx *c, T **p, size_t n)
 
 void free_all(muca_ctx *c)
 {
-    void *dp[] = {c->d_lat, c->d_ej, c->d_edel, c->d_mag, c->d_lnw, c->d_pacc, c->d_w32, c->d_hist,
+    void *dp[] = {c->d_lat, c->d_ej, c->d_edel, c->d_mag, c->d_lnw, c->d_lnw_obs, c->d_pacc, c->d_w32, c->d_hist,
                   c->d_index, c->d_naver, c->d_stats, c->d_ctl, c->d_recs, c->d_obs_part, c->d_obs_out,
                   c->d_jk, c->d_tmp, c->d_bad, c->d_err};
     for (void *p : dp)
@@ -259,6 +259,8 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
     CREATE_TRY(dmalloc(c, &c->d_mag, c->nchains));
     CREATE_TRY(dmalloc(c, &c->d_lnw, (size_t)N + 1));
     CREATE_TRY(dmalloc(c, &c->d_pacc, (size_t)N + 1));
+    CREATE_TRY(dmalloc(c, &c->d_lnw_obs, (size_t)N + 1));
+    CREATE_TRY(cudaMemsetAsync(c->d_lnw_obs, 0, ((size_t)N + 1) * 8, c->stream));
     CREATE_TRY(dmalloc(c, &c->d_w32, (size_t)N + 1));
     CREATE_TRY(dmalloc(c, &c->d_hist, c->hist_len));
     CREATE_TRY(dmalloc(c, &c->d_stats, 1));
@@ -416,6 +418,7 @@ muca_status muca_set_weights(muca_ctx *c, const double *lnw, size_t n)
         if (!std::isfinite(lnw[i])) return fail(c, MUCA_ERR_BAD_ARG, "weight %zu is not finite", i);
     CUDA_TRY(c, cudaSetDevice(c->device));
     CUDA_TRY(c, cudaMemcpyAsync(c->d_lnw, lnw, n * 8, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_lnw_obs, c->d_lnw, n * 8, cudaMemcpyDeviceToDevice, c->stream));
     CUDA_TRY(c, launch_weights_to_f32(c->d_lnw, c->d_w32, (uint32_t)n, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return MUCA_OK;
@@ -518,8 +521,8 @@ muca_status muca_update_weights(muca_ctx *c, uint32_t rule, muca_hist_stats *st)
     return update_impl(c, (int)rule, st);
 }
 
-muca_status muca_weight_run(muca_ctx *c, const muca_run_opts *o, muca_run_result *res, muca_iter_record *recs,
-                            size_t cap)
+static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result *res, muca_iter_record *recs,
+                            size_t cap, muca_iter_callback cb, void *user)
 {
     if (!c || !o) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
     if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "weight run needs a weight-mode context");
@@ -531,17 +534,18 @@ muca_status muca_weight_run(muca_ctx *c, const muca_run_opts *o, muca_run_result
         if (muca_status st = muca_init_chains(c, o->init_scheme, o->jack)) return st;
     }
     const uint32_t max_iter = o->max_iter ? o->max_iter : 1000000u;
-    if (cap > 0 && cap > c->recs_cap) {
+    const size_t need = cb ? 1 : cap;  // streaming keeps the latest record only
+    if (need > 0 && need > c->recs_cap) {
         if (c->d_recs) cudaFree(c->d_recs);
         c->d_recs = nullptr;
-        CUDA_TRY(c, dmalloc(c, &c->d_recs, cap));
-        c->recs_cap = cap;
+        CUDA_TRY(c, dmalloc(c, &c->d_recs, need));
+        c->recs_cap = need;
     }
     RunCtl &h = *c->h_ctl;
     std::memset(&h, 0, sizeof h);
     h.st.k = 0;
     h.st.nup = o->starting_M;
-    h.st.width = 10;  // muca_delta_multigpu.cu:314
+    h.st.width = o->width_start ? o->width_start : 10;  // muca_delta_multigpu.cu:314
     h.st.total_run = (unsigned long long)o->starting_M * c->nchains;
     h.N = c->N;
     h.nchains_total = c->nchains;
@@ -552,8 +556,9 @@ muca_status muca_weight_run(muca_ctx *c, const muca_run_opts *o, muca_run_result
     h.sched = o->nup_schedule;
     h.mom_thr = o->min_over_mean > 0 ? o->min_over_mean : 0.5;
     h.dkl_max = o->d_kl_max > 0 ? o->d_kl_max : 1e-4;
-    h.recs = cap ? c->d_recs : nullptr;
-    h.rec_cap = (uint32_t)cap;
+    h.recs = need ? c->d_recs : nullptr;
+    h.rec_cap = (uint32_t)need;
+    h.rec_ring = cb ? 1u : 0u;
     CUDA_TRY(c, cudaMemcpyAsync(c->d_ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->stream));
     const uint64_t therm = o->therm ? o->therm : c->N;  // therm_coeff * N (:315-316)
     SweepArgs a = sweep_args(c, 0, 100u, 1000u, therm, 0);  // seed SEED+1000*l (:393)
@@ -588,6 +593,17 @@ muca_status muca_weight_run(muca_ctx *c, const muca_run_opts *o, muca_run_result
         mms.push_back(ms);
         tk += ks;
         tm += ms;
+        if (cb) {
+            // this iteration's record lies in the device record array (capacity >= 1 in stream mode)
+            IterRecordDev r;
+            if (cudaMemcpy(&r, c->d_recs, sizeof r, cudaMemcpyDeviceToHost) == cudaSuccess) {
+                muca_iter_record ur{};
+                ur.k = r.k; ur.width_temp = r.width_temp; ur.width = r.width; ur.nupdates = r.nupdates;
+                ur.total_run = r.total_run; ur.d_kl = r.d_kl; ur.min_over_mean = r.min_over_mean;
+                ur.kernel_ms = ks; ur.memcpy_ms = ms;
+                cb(&ur, user);
+            }
+        }
         ++k_done;
         if (h.st.reach && nwidth_time < 0) nwidth_time = tk;
         if (h.st.stop) break;
@@ -627,12 +643,34 @@ muca_status muca_weight_run(muca_ctx *c, const muca_run_opts *o, muca_run_result
     return h.st.converged ? MUCA_OK : fail(c, MUCA_ERR_NOT_CONVERGED, "not converged after %u iterations", k_done);
 }
 
+muca_status muca_weight_run(muca_ctx *c, const muca_run_opts *o, muca_run_result *res, muca_iter_record *recs,
+                            size_t cap)
+{
+    return run_impl(c, o, res, recs, cap, nullptr, nullptr);
+}
+
+muca_status muca_weight_run_stream(muca_ctx *c, const muca_run_opts *o, muca_run_result *res, muca_iter_callback cb,
+                                   void *user)
+{
+    if (!cb) return fail(c, MUCA_ERR_BAD_ARG, "callback is NULL");
+    return run_impl(c, o, res, nullptr, 0, cb, user);
+}
+
 muca_status muca_weight_shift(muca_ctx *c, double beta, double delta)
 {
     if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
     CUDA_TRY(c, cudaSetDevice(c->device));
-    CUDA_TRY(c, launch_weight_shift(c->d_lnw, c->N, beta, delta, c->stream));
-    if (c->mode == MUCA_MODE_WEIGHT) CUDA_TRY(c, launch_weights_to_f32(c->d_lnw, c->d_w32, c->N + 1, c->stream));
+    CUDA_TRY(c, launch_weight_shift(c->d_lnw_obs, c->N, beta, delta, c->stream));
+    return MUCA_OK;
+}
+
+muca_status muca_get_reweighting_weights(muca_ctx *c, double *lnw, size_t n)
+{
+    if (!c || !lnw) return fail(c, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (n != (size_t)c->N + 1) return fail(c, MUCA_ERR_BAD_ARG, "n=%zu, expected N+1=%u", n, c->N + 1);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemcpyAsync(lnw, c->d_lnw_obs, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return MUCA_OK;
 }
 
@@ -645,7 +683,7 @@ muca_status muca_compute_observables(muca_ctx *c, double beta, double delta, muc
         CUDA_TRY(c, dmalloc(c, &c->d_obs_part, observables_partials(c->N)));
         CUDA_TRY(c, dmalloc(c, &c->d_obs_out, 4));
     }
-    CUDA_TRY(c, launch_observables(c->d_hist, c->d_lnw, c->N, beta, delta, c->d_obs_part, c->d_obs_out, c->stream));
+    CUDA_TRY(c, launch_observables(c->d_hist, c->d_lnw_obs, c->N, beta, delta, c->d_obs_part, c->d_obs_out, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(c->h_obs_out, c->d_obs_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     const double s = c->h_obs_out[0], m1 = c->h_obs_out[1], m2 = c->h_obs_out[2], m4 = c->h_obs_out[3];

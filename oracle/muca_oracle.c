@@ -549,7 +549,7 @@ unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int3
     unsigned N = o->L * o->L;
     float *w = (float *)malloc(sizeof(float) * (N + 1));
     uint64_t *h = (uint64_t *)malloc(sizeof(uint64_t) * (N + 1));
-    unsigned width = 10, NUPDATES = o->starting_M;
+    unsigned width = o->width_start ? o->width_start : 10, NUPDATES = o->starting_M;
     int reach = 0;
     uint64_t total_run = 0;
     *converged = 0;

@@ -111,6 +111,7 @@ typedef struct orc_weight_opts {
     unsigned max_iter;
     unsigned rounds;
     int nthreads;
+    unsigned width_start; /* initial running width; 0 = 10 (the reference keeps the previous jack's) */
 } orc_weight_opts;
 unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int32_t *edel,
                         double *lnw, double *p_acc, double *rec, unsigned rec_cap, int *converged);

@@ -1,0 +1,145 @@
+"""The drop-in executables multigpu_weight and produce_gpu: command line,
+output files and their contents against the oracle's restatement of the
+reference programs' main loops (muca_delta_multigpu.cu:87-546,
+produce2_multigpu.cu:91-363)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BIN = os.path.join(ROOT, "muca_gb300", "_build")
+
+
+@pytest.fixture(scope="module")
+def exes():
+    from muca_gb300 import build as b
+    b.build()
+    return os.path.join(BIN, "multigpu_weight"), os.path.join(BIN, "produce_gpu")
+
+
+def test_usage_and_bad_arguments(exes):
+    for exe in exes:
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([exes[0], "8", "1", "0", "1", "1", "0", "0"], capture_output=True, text=True)
+    assert r.returncode == 2  # last_gpu < starting_gpu
+
+
+def test_no_gpu_fails_loudly(exes, tmp_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    r = subprocess.run([exes[0], "8", "0", "0", "1", "1", "0", "0", "--max-iter=2"], capture_output=True,
+                       text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "error" in r.stderr
+
+
+@pytest.mark.gpu
+def test_multigpu_weight_matches_oracle(exes, orc, tmp_path):
+    L, NW, jacks = 4, 256, 2
+    N = L * L
+    r = subprocess.run([exes[0], str(L), "0", "0", str(jacks), "1", "0", "0", "--chains=%d" % NW,
+                        "--max-iter=3000"], capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stderr
+    d = tmp_path / "fss" / ("L%d" % L)
+    files = sorted(os.listdir(d))
+    # the reference appends each jack's log name to one stringstream (:327,367),
+    # so only jack 0's log can be opened; the weight file is written per jack
+    short = [f for f in files if f.startswith("shortiter")]
+    assert short == ["shortiter_gpu1_T050c%d_M1_therm1N_Jack0_iterupdate1.01_rand.txt" % NW]
+    lines = (d / short[0]).read_text().splitlines()
+    assert lines[0] == "#iter width D_KL mcs_time memcpy_time accumulated_time NUPDATES acc_NUP"
+    rows = [ln.split() for ln in lines[1:]]
+
+    # oracle: jack 0 then jack 1 with the weights and width carried over
+    o = orc.WeightOpts(L=L, nchains=NW, jack=0, gpu=0, starting_M=1, recursive=0, hold_until_full=0,
+                       flat_minmean=0, max_iter=3000, rounds=7, nthreads=8, width_start=0)
+    lnw = np.zeros(N + 1)
+    pacc = np.zeros(N + 1)
+    rec = np.zeros(5 * 3000)
+    conv = ctypes.c_int()
+    lat = orc.init_lattice(L, NW, orc.scheme_weight(0, 0)).reshape(-1).copy()
+    ej, ed, _ = orc.energies(L, lat.reshape(NW, N))
+    it = orc.lib().orc_weight_run(ctypes.byref(o), lat, ej, ed, lnw, pacc, rec, 3000, ctypes.byref(conv))
+    assert conv.value == 1
+    assert len(rows) == it
+    rec = rec.reshape(-1, 5)
+    for k, row in enumerate(rows):
+        assert int(row[0]) == k
+        assert int(row[1]) == int(rec[k, 0])
+        np.testing.assert_allclose(float(row[2]), rec[k, 1], rtol=2e-5)
+        assert int(row[6]) == int(rec[k, 2]) and int(row[7]) == int(rec[k, 3])
+    w0 = np.loadtxt(d / ("weight_gpu1_T050c%d_M1_therm1N_JACK0_DKL1e-4_iterupdate1.01_rand.txt" % NW))
+    np.testing.assert_array_equal(w0[:, 0], np.arange(N + 1))
+    np.testing.assert_allclose(w0[:, 1], lnw, rtol=1e-9, atol=1e-9)
+    # jack 1: fresh chains (key 10W + 2), weights and width of jack 0
+    o.jack = 1
+    o.width_start = N
+    lat = orc.init_lattice(L, NW, orc.scheme_weight(1, 0)).reshape(-1).copy()
+    ej, ed, _ = orc.energies(L, lat.reshape(NW, N))
+    orc.lib().orc_weight_run(ctypes.byref(o), lat, ej, ed, lnw, pacc, rec, 3000, ctypes.byref(conv))
+    w1 = np.loadtxt(d / ("weight_gpu1_T050c%d_M1_therm1N_JACK1_DKL1e-4_iterupdate1.01_rand.txt" % NW))
+    np.testing.assert_allclose(w1[:, 1], lnw, rtol=1e-9, atol=1e-9)
+    res = [f for f in files if f.startswith("converge_result")]
+    assert res == ["converge_result_gpu1_T050c%dM1_therm1N_iterupdate1.01_rand.txt" % NW]
+    assert "D_KL is below 1e-4" in r.stdout and "E_DELTA : " in r.stdout
+
+
+def _produce_restated(orc, L, NW, ndev, rng_, tm, nm, delta0, gap, lnw_file):
+    """produce2_multigpu.cu main (:91-363) restated with oracle routines."""
+    Lb = orc.lib()
+    N = L * L
+    beta = 2.0
+    lnw_host = lnw_file.copy()
+    lats, ejs, eds, mgs = [], [], [], []
+    for g in range(ndev):
+        lat = orc.init_lattice(L, NW, orc.scheme_produce(g)).copy()
+        ej, ed, mg = orc.energies(L, lat)
+        lats.append(lat); ejs.append(ej); eds.append(ed); mgs.append(mg)
+    out = []
+    delta = delta0
+    for l in range(rng_):
+        delta = delta + gap / rng_
+        Lb.orc_weight_shift(beta, delta, N, lnw_host)
+        bz = np.zeros(N + 1)
+        Lb.orc_boltz(beta, delta, N, lnw_host, bz, 0)
+        mj, sj = [], []
+        for g in range(ndev):
+            lats[g], _ = orc.produce_sweep(L, lats[g], ejs[g], eds[g], mgs[g], lnw_file, 0, 100 + 1000 * g + l,
+                                           N * tm, 0, nthreads=8)
+        for g in range(ndev):
+            lats[g], h = orc.produce_sweep(L, lats[g], ejs[g], eds[g], mgs[g], lnw_file, l, 100 + 2000 * g, 0,
+                                           N * nm, nthreads=8)
+            o = orc.observables(beta, N, h, bz)
+            mj.append(o[0]); sj.append(o[1])
+        out.append((orc.jackknife(np.array(mj)), orc.jackknife(np.array(sj))))
+    return out
+
+
+@pytest.mark.gpu
+def test_produce_gpu_matches_oracle(exes, orc, tmp_path):
+    L, NW, ndev, rng_, tm, nm = 4, 256, 2, 3, 20, 40
+    N = L * L
+    d = tmp_path / "fss" / ("L%d" % L)
+    d.mkdir(parents=True)
+    rng = np.random.default_rng(9)
+    lnw = np.cumsum(rng.normal(-0.8, 0.4, N + 1))
+    lnw -= lnw[0]
+    with open(d / "weight_mpi_T050c16_M200_JACK0_DKL1e-4.txt", "w") as f:
+        for i, v in enumerate(lnw):
+            f.write("%d %.10g\n" % (i, v))
+    lnw_file = np.array([float("%.10g" % v) for v in lnw])
+    args = [str(L), "0", str(ndev - 1), str(rng_), "5", str(tm), str(nm), "1.9", "0.1"]
+    r = subprocess.run([exes[1]] + args + ["--chains=%d" % NW], capture_output=True, text=True, cwd=tmp_path,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    name = "observables_gpu%d_T050_JACKgpu_THERM%sN_NUP%sN_delta1.9to0.1noreset.txt" % (ndev, tm, nm)
+    rows = [list(map(float, ln.split())) for ln in (d / name).read_text().splitlines()]
+    exp = _produce_restated(orc, L, NW, ndev, rng_, tm, nm, 1.9, 0.1, lnw_file)
+    assert len(rows) == rng_
+    for i, ((m, s), row) in enumerate(zip(exp, rows)):
+        np.testing.assert_allclose(row[0], 1.9 + 0.1 * (i + 1) / rng_, rtol=1e-9)
+        np.testing.assert_allclose(row[1:], [m[0], m[1], s[0], s[1]], rtol=2e-9, atol=1e-12)

@@ -356,7 +356,8 @@ def test_observables_vs_oracle(muca, orc, L, delta):
         e.set_weights(lnw)
         e.set_histogram(h)
         e.weight_shift(beta, delta)
-        shifted = e.get_weights()
+        shifted = e.reweighting_weights()
+        np.testing.assert_array_equal(e.get_weights(), lnw)  # the sweep keeps the weights as set
         ob = e.observables(beta, delta)
     ref = lnw.copy()
     orc.lib().orc_weight_shift(beta, delta, N, ref)
