@@ -137,7 +137,7 @@ def profile_traffic():
         return None
 
 
-def cpu_oracle_rate(L, chains, nthreads, min_seconds=4.0, max_reps=5):
+def cpu_oracle_rate(L, chains, nthreads, min_seconds=12.0, max_reps=200):
     """The reference algorithm on the host: full steps (therm=N, nup=N) of
     `chains` chains with `nthreads` POSIX threads; returns (attempts/ns, sample)."""
     import numpy as np

@@ -264,11 +264,11 @@ class Engine:
 
     def weight_run(self, starting_M=1, jack=0, rule=UPDATE_TRIVIAL, hold_until_full=0, flat_minmean=0,
                    max_iter=0, therm=0, init_scheme=INIT_WEIGHT, reinit_chains=1, nup_schedule=0,
-                   min_over_mean=0.0, d_kl_max=0.0, records=1000, raise_on_not_converged=False):
+                   min_over_mean=0.0, d_kl_max=0.0, width_start=0, records=1000, raise_on_not_converged=False):
         o = RunOpts(jack=jack, starting_M=starting_M, therm=therm, rule=rule, hold_until_full=hold_until_full,
                     flat_minmean=flat_minmean, max_iter=max_iter, init_scheme=init_scheme,
                     reinit_chains=reinit_chains, nup_schedule=nup_schedule, min_over_mean=min_over_mean,
-                    d_kl_max=d_kl_max)
+                    d_kl_max=d_kl_max, width_start=width_start)
         res = RunResult()
         recs = (IterRecord * max(records, 1))()
         st = self._lib.muca_weight_run(self._h, C.byref(o), C.byref(res), recs, records)

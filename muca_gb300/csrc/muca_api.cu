@@ -546,7 +546,11 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     h.st.k = 0;
     h.st.nup = o->starting_M;
     h.st.width = o->width_start ? o->width_start : 10;  // muca_delta_multigpu.cu:314
-    h.st.total_run = (unsigned long long)o->starting_M * c->nchains;
+    // the schedule runs at the top of every iteration (:379-382), so a run that
+    // starts at full width (a later jack) grows NUPDATES before its first sweep;
+    // the device applies it between iterations from then on
+    if (h.st.width == c->N) h.st.nup = o->nup_schedule ? h.st.nup * 2u : (unsigned)((h.st.nup + 1u) * 1.01);
+    h.st.total_run = (unsigned long long)h.st.nup * c->nchains;
     h.N = c->N;
     h.nchains_total = c->nchains;
     h.rule = o->rule;

@@ -162,6 +162,26 @@ static inline void propose(int8_t *s, const uint32_t *nv, unsigned idx, uint32_t
     *new_s = ns;
 }
 
+/* Acceptance logarithm of the GPU kernels: log(u01fixedpt<float>(r)) on the
+ * device is CUDA's logf (muca_delta_multigpu.cu:781,816,
+ * produce2_multigpu.cu:446,481).  Without a table this is libm's logf, which
+ * differs from CUDA's by one ulp for some u; with the table of CUDA's values
+ * (tab[k] for u = (2k+1) 2^-24, k = r >> 9, made by devlogf.cu) the decision
+ * is the device's. */
+static const float *g_logf_tab = NULL;
+
+void orc_set_logf_table(const float *tab) { g_logf_tab = tab; }
+
+void orc_libm_logf_table(float *tab)
+{
+    for (uint32_t k = 0; k < (1u << 23); ++k) tab[k] = logf(orc_u01fixedpt_f32(k << 9));
+}
+
+static inline float accept_logf(uint32_t r)
+{
+    return g_logf_tab ? g_logf_tab[r >> 9] : logf(orc_u01fixedpt_f32(r));
+}
+
 /* Kernel mcs of muca_delta_multigpu.cu:737-829 for one chain. */
 static void weight_chain(unsigned L, const uint32_t *nv, const uint32_t *ix, unsigned W, int8_t *s,
                          int32_t *ej, int32_t *edel, const float *w, uint64_t *hist,
@@ -187,7 +207,7 @@ static void weight_chain(unsigned L, const uint32_t *nv, const uint32_t *ix, uns
             float diff = -dE * 2 + w[E + dDel] - w[E];
             if (diff >= 0) {
                 s[idx] = (int8_t)ns; energy += dE; E += dDel;
-            } else if (logf(orc_u01fixedpt_f32(r1[i % 4])) < diff) {
+            } else if (accept_logf(r1[i % 4]) < diff) {
                 s[idx] = (int8_t)ns; energy += dE; E += dDel;
             } else {
                 s[idx] = (int8_t)os;
@@ -225,7 +245,7 @@ static void produce_chain(unsigned L, const uint32_t *nv, const uint32_t *ix, un
             double diff = -dE * 2 + w[E + dDel] - w[E];
             if (diff >= 0) {
                 s[idx] = (int8_t)ns; energy += dE; E += dDel; M += dM;
-            } else if (logf(orc_u01fixedpt_f32(r1[i % 4])) < diff) {
+            } else if (accept_logf(r1[i % 4]) < diff) {
                 s[idx] = (int8_t)ns; energy += dE; E += dDel; M += dM;
             } else {
                 s[idx] = (int8_t)os;

@@ -57,6 +57,14 @@ void orc_init_lattice(unsigned L, unsigned chain0, unsigned nchains, const orc_i
 /* E_J (computeEnergies, :69-74 + :548-571), E_Delta (:76-83), M (produce2:84-89) */
 void orc_chain_energies(unsigned L, unsigned nchains, const int8_t *lat, int32_t *ej, int32_t *edel, int32_t *mag);
 
+/* Acceptance logarithm of orc_weight_sweep / orc_produce_sweep: NULL = libm
+ * logf; else tab[k] = CUDA's logf((2k+1) 2^-24) for k < 2^23 (devlogf.cu),
+ * the value the reference kernels compute on the device.  The table is read,
+ * not copied: it must stay alive while set. */
+void orc_set_logf_table(const float *tab);
+/* the same table with libm's logf (2^23 floats), to check the lookup */
+void orc_libm_logf_table(float *tab);
+
 /* ---- sweeps ----
  * orc_weight_sweep: muca_delta_multigpu.cu:737-829 (kernel mcs), FP32 weights,
  * histogram of E_Delta after every production attempt (added to hist, u64).

@@ -98,8 +98,40 @@ def lib():
     L.orc_weight_run.argtypes = [C.POINTER(WeightOpts), _i8p, _i32p, _i32p, _f64p, _f64p, _f64p,
                                  C.c_uint, C.POINTER(C.c_int)]
     L.orc_weight_run.restype = C.c_uint
+    L.orc_set_logf_table.argtypes = [C.c_void_p]
+    L.orc_libm_logf_table.argtypes = [_f32p]
     _LIB = L
     return L
+
+
+# --------------------------------------------------------------------------
+# The device's acceptance logarithm (devlogf.cu)
+
+_LOGF_TAB = None
+
+
+def device_logf_table(device: int = 0) -> np.ndarray:
+    """CUDA's logf((2k+1) 2^-24) for k < 2^23, evaluated on `device` (needs a
+    GPU and oracle/_build/libdevlogf.so from build(refgpu=True))."""
+    global _LOGF_TAB
+    if _LOGF_TAB is None:
+        path = os.path.join(BUILD, "libdevlogf.so")
+        if not os.path.exists(path):
+            build(refgpu=True)
+        D = C.CDLL(path)
+        D.orc_device_logf_table.argtypes = [C.c_int, _f32p, C.c_char_p, C.c_int]
+        tab = np.empty(1 << 23, np.float32)
+        err = C.create_string_buffer(256)
+        if D.orc_device_logf_table(device, tab, err, 256) != 0:
+            raise RuntimeError("device logf table: " + err.value.decode())
+        _LOGF_TAB = tab
+    return _LOGF_TAB
+
+
+def use_device_logf(on: bool = True) -> None:
+    """Make the oracle's weight and production sweeps decide with the device's
+    logf (on) or with libm's (off)."""
+    lib().orc_set_logf_table(device_logf_table().ctypes.data if on else None)
 
 
 # --------------------------------------------------------------------------

@@ -24,6 +24,22 @@ def orc():
     return o
 
 
+@pytest.fixture(autouse=True)
+def _device_acceptance_logf(request):
+    """GPU tests compare with what the reference kernels compute on the device,
+    whose acceptance test uses CUDA's logf; the oracle takes the device's logf
+    values for them (libm's logf differs by one ulp for some u).  CPU tests
+    keep libm's, as the reference's CPU programs do."""
+    if request.node.get_closest_marker("gpu") is None:
+        yield
+        return
+    from oracle import orc as o
+    o.build(refgpu=True)
+    o.use_device_logf(True)
+    yield
+    o.use_device_logf(False)
+
+
 @pytest.fixture(scope="session")
 def muca():
     """The engine, built for sm_103a; GPU tests only."""

@@ -341,6 +341,49 @@ def test_weight_run_vs_oracle(muca, orc, rule, hold, flat):
     np.testing.assert_allclose(w, lnw, rtol=1e-12, atol=1e-9)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("L", [4, 8])
+def test_weight_run_later_jack_vs_oracle(muca, orc, L):
+    """A second jack as the reference's jack loop runs it (muca_delta_multigpu.cu:336-382):
+    fresh chains with key 10W + 2*mm, NUPDATES back at starting_M, the weights
+    and the running width of the previous jack kept -- so the schedule grows
+    NUPDATES before the first sweep."""
+    cpd, max_iter = 256, 3000
+    N = L * L
+    o = orc.WeightOpts(L=L, nchains=cpd, jack=0, gpu=0, starting_M=1, recursive=0, hold_until_full=0,
+                       flat_minmean=0, max_iter=max_iter, rounds=7, nthreads=8, width_start=0)
+    lnw = np.zeros(N + 1)
+    pacc = np.zeros(N + 1)
+    rec = np.zeros(5 * max_iter)
+    conv = ctypes.c_int()
+    with muca.Engine(L, nchains=cpd) as e:
+        r0, _ = e.weight_run(starting_M=1, jack=0, max_iter=max_iter, records=1)
+        olat = orc.init_lattice(L, cpd, orc.scheme_weight(0, 0)).reshape(-1).copy()
+        oej, oed, _ = orc.energies(L, olat.reshape(cpd, N))
+        it0 = orc.lib().orc_weight_run(ctypes.byref(o), olat, oej, oed, lnw, pacc, rec, max_iter,
+                                       ctypes.byref(conv))
+        assert conv.value == 1 and r0.converged == 1 and r0.iterations == it0
+        np.testing.assert_allclose(e.get_weights(), lnw, rtol=1e-12, atol=1e-9)
+        res, recs = e.weight_run(starting_M=1, jack=1, max_iter=max_iter, width_start=N, records=max_iter)
+        lat = e.get_lattice()
+        w = e.get_weights()
+    o.jack = 1
+    o.width_start = N
+    olat = orc.init_lattice(L, cpd, orc.scheme_weight(1, 0)).reshape(-1).copy()
+    oej, oed, _ = orc.energies(L, olat.reshape(cpd, N))
+    rec[:] = 0
+    it = orc.lib().orc_weight_run(ctypes.byref(o), olat, oej, oed, lnw, pacc, rec, max_iter, ctypes.byref(conv))
+    rec = rec.reshape(max_iter, 5)
+    for k, r in enumerate(recs[:it]):
+        assert r.nupdates == int(rec[k, 2]), k
+        assert r.total_run == int(rec[k, 3]), k
+        assert r.width_temp == int(rec[k, 0]), k
+        np.testing.assert_allclose(r.d_kl, rec[k, 1], rtol=1e-10, atol=1e-15, err_msg="iteration %d" % k)
+    assert res.iterations == it and res.converged == conv.value
+    np.testing.assert_array_equal(lat, olat.reshape(cpd, N))
+    np.testing.assert_allclose(w, lnw, rtol=1e-12, atol=1e-9)
+
+
 # ---- production reweighting ----------------------------------------------------------------
 
 @pytest.mark.parametrize("L,delta", [(4, 1.96), (8, 1.5), (16, 1.99)])

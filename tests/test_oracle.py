@@ -55,6 +55,36 @@ def test_u01_exhaustive_direction_and_init(orc):
         assert (L.orc_u01fixedpt_f32(r) < 0.5) == (r < (1 << 31))
 
 
+def test_acceptance_logf_table_lookup(orc):
+    """The table path of the acceptance logarithm: entry r >> 9 holds the value
+    for u01fixedpt<float>(r) = (2k+1) 2^-24, so a table of libm's values
+    reproduces the libm path exactly, and a planted table changes decisions."""
+    L = orc.lib()
+    rng = np.random.default_rng(5)
+    for r in rng.integers(0, 1 << 32, 20000, dtype=np.uint64):
+        r = int(r)
+        assert np.float32(L.orc_u01fixedpt_f32(r)) == np.float32((2 * (r >> 9) + 1) * 2.0 ** -24)
+    tab = np.empty(1 << 23, np.float32)
+    L.orc_libm_logf_table(tab)
+    Ls, n = 8, 16
+    N = Ls * Ls
+    w32 = (np.cumsum(rng.normal(-0.9, 0.3, N + 1))).astype(np.float32)
+    lat0 = orc.init_lattice(Ls, n, orc.scheme_weight(0, 0))
+    ej0, ed0, _ = orc.energies(Ls, lat0)
+    outs = []
+    for t in (None, tab, np.full(1 << 23, -np.inf, np.float32)):
+        L.orc_set_logf_table(None if t is None else t.ctypes.data)
+        try:
+            ej, ed = ej0.copy(), ed0.copy()
+            lat, h = orc.weight_sweep(Ls, lat0.copy(), ej, ed, w32, 3, 100, N, 4 * N)
+        finally:
+            L.orc_set_logf_table(None)
+        outs.append((lat, h, ed))
+    for a, b in zip(outs[0], outs[1]):
+        np.testing.assert_array_equal(a, b)
+    assert not np.array_equal(outs[0][1], outs[2][1])
+
+
 def test_sweep_tables(orc):
     for L in (2, 4, 6, 8, 72):
         nv, ix = orc.tables(L)
