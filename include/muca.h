@@ -218,6 +218,23 @@ muca_status muca_weight_run_stream(muca_ctx *ctx, const muca_run_opts *opts, muc
 muca_status muca_weight_shift(muca_ctx *ctx, double beta, double delta);
 muca_status muca_get_reweighting_weights(muca_ctx *ctx, double *lnw, size_t n);
 muca_status muca_compute_observables(muca_ctx *ctx, double beta, double delta, muca_observables *out);
+/* No counterpart in the reference.  The four reweighting sums of
+ * muca_compute_observables -- d_sums[0..3] = {sum, m1, m2, m4} -- over a
+ * triangular (E_Delta, M) histogram d_hist2d ((N+1)(N+2)/2 u64, N = L*L) and
+ * weights d_lnw (N+1 doubles, already shifted as the caller wants), all
+ * device buffers owned by the caller; no context.  The call allocates
+ * nothing: for callers that must not see a device allocation (a scheduler
+ * owning HBM through its own pool and budget; a process that only reweights
+ * histograms it holds).  Its scratch is a fixed device array of 608 x 4
+ * doubles inside the library, whose address is looked up on the first call
+ * per device; make that first call before any stream capture, since it may
+ * load the module.  Nothing needs to start at zero.  Two calls in flight at
+ * once on the same device share that array and race.  L outside 2..128 is
+ * rejected with MUCA_ERR_BAD_ARG.  The work is enqueued on `stream`
+ * (cudaStream_t, NULL = the legacy default stream); d_sums is valid once the
+ * stream reaches it.  Errors: muca_last_error(NULL). */
+muca_status muca_observables_noalloc(int32_t device, const uint64_t *d_hist2d, const double *d_lnw, uint32_t L,
+                                    double beta, double delta, double *d_sums, void *stream);
 /* Leave-one-out jackknife (muca_delta_multigpu.cu:620-635) on the device. */
 muca_status muca_jackknife(muca_ctx *ctx, const double *x, uint32_t n, double *avg, double *err);
 

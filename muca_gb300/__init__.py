@@ -34,6 +34,7 @@ EXPORTS = [
     "muca_clear_histogram", "muca_get_histogram", "muca_set_histogram", "muca_histogram_stats", "muca_update_weights",
     "muca_weight_run", "muca_weight_shift", "muca_compute_observables", "muca_jackknife",
     "muca_philox_peak", "muca_weight_run_stream", "muca_get_reweighting_weights",
+    "muca_observables_noalloc",
 ]
 
 
@@ -136,6 +137,7 @@ def lib():
     L.muca_compute_observables.argtypes = [vp, C.c_double, C.c_double, C.POINTER(Observables)]
     L.muca_jackknife.argtypes = [vp, f64, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.muca_philox_peak.argtypes = [C.c_int32, C.c_uint32, C.POINTER(C.c_double)]
+    L.muca_observables_noalloc.argtypes = [C.c_int32, vp, vp, C.c_uint32, C.c_double, C.c_double, vp, vp]
     _LIB = L
     return L
 
@@ -147,6 +149,15 @@ def philox_peak(device: int = 0, rounds: int = 7) -> float:
     if st:
         raise MucaError(st, lib().muca_last_error(None).decode())
     return out.value
+
+
+def observables_noalloc(device, d_hist2d, d_lnw, L, beta, delta, d_sums, stream=None) -> None:
+    """muca_observables_noalloc on raw device addresses (ints): the four
+    reweighting sums into d_sums, enqueued on `stream` (a cudaStream_t as int,
+    None = the legacy default stream); nothing is allocated."""
+    st = lib().muca_observables_noalloc(device, d_hist2d, d_lnw, L, beta, delta, d_sums, stream)
+    if st:
+        raise MucaError(st, lib().muca_last_error(None).decode())
 
 
 def default_chains(device: int = 0) -> int:

@@ -16,6 +16,8 @@
 #include "muca_device.cuh"
 #include "muca_internal.h"
 
+#include <mutex>
+
 namespace muca {
 
 constexpr int kObsThreads = 256;
@@ -152,6 +154,57 @@ cudaError_t launch_jackknife(const double *x, uint32_t n, double *out2, cudaStre
 {
     k_jackknife<<<1, 32, 0, s>>>(x, n, out2);
     return cudaGetLastError();
+}
+
+// ---- the reweighting sums without any allocation ------------------------
+//
+// Some callers cannot let this library allocate device memory.  Example: a
+// scheduler that packs many production instances into a fixed HBM budget
+// through its own pool, where a hidden cudaMalloc would break the budget and
+// also synchronise the device under the scheduler's other streams.  Another:
+// a process that only reweights histograms it already holds on the device.
+// It has no lattice and so no engine context, whose creation allocates.  For
+// them, the two kernels above run with their block partials in the
+// file-scope array below instead of context memory.
+//
+// The array holds the partials of the fixed kObsBlocks-block grid,
+// kObsBlocks x 4 doubles (19,456 bytes), whatever L is.  Each block
+// overwrites its own four entries before the final pass reads them, so
+// nothing in it has to start at zero, and no state carries from one call to
+// the next.  There is one array per device, shared by every caller in the
+// process: two calls in flight at once on the same device (two streams, or
+// two host threads) write the same entries and race.
+constexpr size_t kStaticPartials = (size_t)kObsBlocks * 4;
+static __device__ __align__(256) double g_obs_partials[kStaticPartials];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_partials_mu;
+double *g_partials_addr[kMaxDevices] = {};
+}  // namespace
+
+size_t observables_static_partials() { return kStaticPartials; }
+
+cudaError_t launch_observables_static(int device, const unsigned long long *hist2d, const double *lnw, uint32_t N,
+                                      double beta, double delta, double *out, cudaStream_t s)
+{
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    if (observables_partials(N) > kStaticPartials) return cudaErrorInvalidValue;
+    double *partials = nullptr;
+    {
+        // The address is resolved once per device, with that device current
+        // (the caller has made it current).  The first resolution may load
+        // this module onto the device.
+        std::lock_guard<std::mutex> lock(g_partials_mu);
+        if (!g_partials_addr[device]) {
+            void *p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_obs_partials);
+            if (e != cudaSuccess) return e;
+            g_partials_addr[device] = static_cast<double *>(p);
+        }
+        partials = g_partials_addr[device];
+    }
+    return launch_observables(hist2d, lnw, N, beta, delta, partials, out, s);
 }
 
 }  // namespace muca

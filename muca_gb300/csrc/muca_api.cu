@@ -722,6 +722,21 @@ muca_status muca_jackknife(muca_ctx *c, const double *x, uint32_t n, double *avg
     return MUCA_OK;
 }
 
+muca_status muca_observables_noalloc(int32_t device, const uint64_t *d_hist2d, const double *d_lnw, uint32_t L,
+                                    double beta, double delta, double *d_sums, void *stream)
+{
+    if (!d_hist2d || !d_lnw || !d_sums) return fail(nullptr, MUCA_ERR_BAD_ARG, "NULL device pointer");
+    if (L < 2 || L > 128) return fail(nullptr, MUCA_ERR_BAD_ARG, "L=%u outside 2..128", L);
+    const uint32_t N = L * L;
+    if (observables_partials(N) > observables_static_partials())
+        return fail(nullptr, MUCA_ERR_BAD_ARG, "L=%u needs %zu doubles of scratch; the static array holds %zu", L,
+                    observables_partials(N), observables_static_partials());
+    CUDA_TRY(nullptr, cudaSetDevice(device));
+    CUDA_TRY(nullptr, launch_observables_static(device, reinterpret_cast<const unsigned long long *>(d_hist2d), d_lnw,
+                                                N, beta, delta, d_sums, static_cast<cudaStream_t>(stream)));
+    return MUCA_OK;
+}
+
 muca_status muca_philox_peak(int32_t device, uint32_t rounds, double *blocks_per_s)
 {
     if (!blocks_per_s) return fail(nullptr, MUCA_ERR_BAD_ARG, "NULL argument");

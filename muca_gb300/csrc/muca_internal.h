@@ -133,6 +133,12 @@ size_t observables_partials(uint32_t N);
 cudaError_t launch_observables(const unsigned long long *hist2d, const double *lnw, uint32_t N, double beta,
                                double delta, double *partials, double *out, cudaStream_t s);
 cudaError_t launch_jackknife(const double *x, uint32_t n, double *out2, cudaStream_t s);
+// The same sums with the partials in a file-scope device array of
+// observables_static_partials() doubles (no allocation); `device` must be the
+// current device.  Calls in flight at once on one device race on that array.
+size_t observables_static_partials();
+cudaError_t launch_observables_static(int device, const unsigned long long *hist2d, const double *lnw, uint32_t N,
+                                      double beta, double delta, double *out, cudaStream_t s);
 
 // Philox throughput microbenchmark (k_bench.cu): grid blocks of 256 threads,
 // each generating blocks_per_thread Philox4x32-R blocks.
