@@ -243,6 +243,91 @@ muca_status muca_jackknife(muca_ctx *ctx, const double *x, uint32_t n, double *a
  * integer-pipe ceiling against which the sweep kernels are reported. */
 muca_status muca_philox_peak(int32_t device, uint32_t rounds, double *blocks_per_s);
 
+/* ---- Batches of independent weight runs (no counterpart in the reference) ----
+ * The reference estimates one (L, T) weight per program run.  A batch runs
+ * many such estimations of uneven size together on one GPU: every iteration
+ * sweeps all running instances in one persistent kernel and updates each
+ * instance's FP64 weights on the device; the iteration loop is captured
+ * into a CUDA graph and replayed until every instance has stopped.
+ * Instance i is the reference weight loop (muca_delta_multigpu.cu:374-477)
+ * for its L and beta with the seeds of emulated device `seed`: initial spins
+ * from key {10W, 0xdecafbad}, counter {2*seed, 100, 0xBADCAB1E, 0xBADC0DED};
+ * sweep counter word 1 = 100 + 1000*seed.  With beta = 2 its results equal a
+ * single context's (muca_params.dev_offset = seed, same L and nchains).
+ * Any other beta replaces the reference's -2 dE (T = 0.5, :810) by the
+ * FP32 value (float)(-beta*dE). */
+typedef struct muca_batch muca_batch;
+
+typedef struct muca_instance {
+    uint32_t L;        /* 8..128, a multiple of 8 */
+    uint32_t nchains;  /* 1..65536 */
+    uint32_t seed;     /* emulated device index of the instance's streams */
+    uint32_t reserved;
+    double beta;       /* 1/T > 0; 2 is the reference's fixed T = 0.5 */
+} muca_instance;
+
+typedef struct muca_batch_shape {
+    uint32_t chains_per_block;  /* 32, 64, 128 or 256 */
+    uint32_t lattice_in_smem;   /* packed lattice staged in shared memory */
+    uint32_t hist_in_smem;      /* u32 histogram bins in shared memory (else u64 device atomics) */
+    uint32_t blocks_per_sm;     /* resident blocks of the persistent grid per SM */
+    double ms;                  /* autotuner: one sweep (therm N + nup N) of the whole batch */
+} muca_batch_shape;
+
+typedef struct muca_batch_params {
+    int32_t device;
+    uint32_t rounds;                 /* Philox rounds: 7 (reference) or 10 */
+    void *stream;                    /* cudaStream_t; NULL = own stream */
+    uint32_t shape_chains_per_block; /* 0 = autotune; else this fixed shape: */
+    uint32_t shape_lattice_in_smem;
+    uint32_t shape_hist_in_smem;
+} muca_batch_params;
+
+typedef struct muca_batch_info {
+    uint32_t n_instances, n_items, grid, threads, smem_bytes, n_tried;
+    muca_batch_shape shape;     /* in use */
+    muca_batch_shape tried[32]; /* the autotuner's table (n_tried entries) */
+    uint64_t device_bytes;
+    double log_bracket;
+} muca_batch_info;
+
+typedef struct muca_batch_run_opts {
+    uint32_t starting_M;    /* initial NUPDATES of every instance */
+    uint32_t rule;          /* muca_update_rule */
+    uint32_t nup_schedule;  /* 0: (NUP+1)*1.01 once width == N (:379-382); 1: doubling */
+    uint32_t flat_minmean;  /* 0: stop at width == N && D_KL < d_kl_max; 1: at min/mean >= min_over_mean */
+    uint32_t max_iter;      /* per instance (0 = 1000000) */
+    uint32_t graph_iters;   /* iterations per captured graph (0 = 16) */
+    uint32_t reinit_chains; /* 1: initial spins again before the run */
+    uint32_t reserved;
+    double min_over_mean;   /* 0 = 0.5 */
+    double d_kl_max;        /* 0 = 1e-4 */
+} muca_batch_run_opts;
+
+typedef struct muca_batch_result {
+    uint32_t iterations, converged, width, reach_iter, nupdates, reserved;
+    uint64_t total_run;     /* attempts counted by the reference's acc_NUP: sum of NUPDATES * nchains */
+    double d_kl, min_over_mean;  /* of the last iteration */
+} muca_batch_result;
+
+/* Creates the batch, chooses the block shape (autotuner unless fixed) and
+ * initialises the chains; weights start at zero. */
+muca_status muca_batch_create(const muca_batch_params *params, const muca_instance *inst, uint32_t n,
+                              muca_batch **out);
+muca_status muca_batch_destroy(muca_batch *b);
+const char *muca_batch_last_error(const muca_batch *b); /* NULL: errors of muca_batch_create */
+muca_status muca_batch_get_info(const muca_batch *b, muca_batch_info *info);
+muca_status muca_batch_init_chains(muca_batch *b);
+/* Weights of instance i (N+1 values; the warm start of a run) and its results. */
+muca_status muca_batch_set_weights(muca_batch *b, uint32_t i, const double *lnw, size_t n);
+muca_status muca_batch_get_weights(muca_batch *b, uint32_t i, double *lnw, size_t n);
+muca_status muca_batch_get_histogram(muca_batch *b, uint32_t i, uint64_t *hist, size_t n);
+/* Runs every instance to its stop criterion or max_iter; res (n entries,
+ * may be NULL) gets each instance's outcome, *seconds (may be NULL) the
+ * device time.  MUCA_ERR_NOT_CONVERGED if some instance hit max_iter. */
+muca_status muca_batch_run(muca_batch *b, const muca_batch_run_opts *opts, muca_batch_result *res,
+                           double *seconds);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,6 +35,9 @@ EXPORTS = [
     "muca_weight_run", "muca_weight_shift", "muca_compute_observables", "muca_jackknife",
     "muca_philox_peak", "muca_weight_run_stream", "muca_get_reweighting_weights",
     "muca_observables_noalloc",
+    "muca_batch_create", "muca_batch_destroy", "muca_batch_last_error", "muca_batch_get_info",
+    "muca_batch_init_chains", "muca_batch_set_weights", "muca_batch_get_weights", "muca_batch_get_histogram",
+    "muca_batch_run",
 ]
 
 
@@ -89,6 +92,41 @@ class RunResult(C.Structure):
 ITER_CB = C.CFUNCTYPE(None, C.POINTER(IterRecord), C.c_void_p)
 
 
+class Instance(C.Structure):
+    _fields_ = [("L", C.c_uint32), ("nchains", C.c_uint32), ("seed", C.c_uint32), ("reserved", C.c_uint32),
+                ("beta", C.c_double)]
+
+
+class BatchShape(C.Structure):
+    _fields_ = [("chains_per_block", C.c_uint32), ("lattice_in_smem", C.c_uint32), ("hist_in_smem", C.c_uint32),
+                ("blocks_per_sm", C.c_uint32), ("ms", C.c_double)]
+
+
+class BatchParams(C.Structure):
+    _fields_ = [("device", C.c_int32), ("rounds", C.c_uint32), ("stream", C.c_void_p),
+                ("shape_chains_per_block", C.c_uint32), ("shape_lattice_in_smem", C.c_uint32),
+                ("shape_hist_in_smem", C.c_uint32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("n_instances", C.c_uint32), ("n_items", C.c_uint32), ("grid", C.c_uint32), ("threads", C.c_uint32),
+                ("smem_bytes", C.c_uint32), ("n_tried", C.c_uint32), ("shape", BatchShape),
+                ("tried", BatchShape * 32), ("device_bytes", C.c_uint64), ("log_bracket", C.c_double)]
+
+
+class BatchRunOpts(C.Structure):
+    _fields_ = [("starting_M", C.c_uint32), ("rule", C.c_uint32), ("nup_schedule", C.c_uint32),
+                ("flat_minmean", C.c_uint32), ("max_iter", C.c_uint32), ("graph_iters", C.c_uint32),
+                ("reinit_chains", C.c_uint32), ("reserved", C.c_uint32), ("min_over_mean", C.c_double),
+                ("d_kl_max", C.c_double)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("converged", C.c_uint32), ("width", C.c_uint32),
+                ("reach_iter", C.c_uint32), ("nupdates", C.c_uint32), ("reserved", C.c_uint32),
+                ("total_run", C.c_uint64), ("d_kl", C.c_double), ("min_over_mean", C.c_double)]
+
+
 class Observables(C.Structure):
     _fields_ = [("m_abs", C.c_double), ("chi", C.c_double), ("u4", C.c_double), ("sum", C.c_double),
                 ("m1", C.c_double), ("m2", C.c_double), ("m4", C.c_double)]
@@ -138,6 +176,16 @@ def lib():
     L.muca_jackknife.argtypes = [vp, f64, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.muca_philox_peak.argtypes = [C.c_int32, C.c_uint32, C.POINTER(C.c_double)]
     L.muca_observables_noalloc.argtypes = [C.c_int32, vp, vp, C.c_uint32, C.c_double, C.c_double, vp, vp]
+    L.muca_batch_create.argtypes = [C.POINTER(BatchParams), C.POINTER(Instance), C.c_uint32, C.POINTER(vp)]
+    L.muca_batch_destroy.argtypes = [vp]
+    L.muca_batch_last_error.argtypes = [vp]
+    L.muca_batch_last_error.restype = C.c_char_p
+    L.muca_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+    L.muca_batch_init_chains.argtypes = [vp]
+    L.muca_batch_set_weights.argtypes = [vp, C.c_uint32, f64, C.c_size_t]
+    L.muca_batch_get_weights.argtypes = [vp, C.c_uint32, f64, C.c_size_t]
+    L.muca_batch_get_histogram.argtypes = [vp, C.c_uint32, u64, C.c_size_t]
+    L.muca_batch_run.argtypes = [vp, C.POINTER(BatchRunOpts), C.POINTER(BatchResult), C.POINTER(C.c_double)]
     _LIB = L
     return L
 
@@ -307,3 +355,84 @@ class Engine:
         a, e = C.c_double(), C.c_double()
         self._ck(self._lib.muca_jackknife(self._h, x, x.size, C.byref(a), C.byref(e)))
         return a.value, e.value
+
+
+
+class Batch:
+    """Many independent weight runs of uneven size on one GPU (muca_batch_*).
+
+    instances: sequence of (L, nchains, beta, seed).  shape: None (autotune)
+    or (chains_per_block, lattice_in_smem, hist_in_smem)."""
+
+    def __init__(self, instances, device=0, rounds=7, stream=None, shape=None):
+        self._lib = lib()
+        self.instances = [tuple(x) for x in instances]
+        arr = (Instance * len(self.instances))()
+        for k, (L, nc, beta, seed) in enumerate(self.instances):
+            arr[k] = Instance(L=L, nchains=nc, seed=seed, reserved=0, beta=beta)
+        p = BatchParams(device=device, rounds=rounds, stream=C.c_void_p(stream) if stream else None)
+        if shape is not None:
+            p.shape_chains_per_block, p.shape_lattice_in_smem, p.shape_hist_in_smem = shape
+        h = C.c_void_p()
+        st = self._lib.muca_batch_create(C.byref(p), arr, len(self.instances), C.byref(h))
+        if st:
+            raise MucaError(st, self._lib.muca_batch_last_error(None).decode())
+        self._h = h
+
+    def _ck(self, st, allow=()):
+        if st and st not in allow:
+            raise MucaError(st, self._lib.muca_batch_last_error(self._h).decode())
+        return st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.muca_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self):
+        o = BatchInfo()
+        self._ck(self._lib.muca_batch_get_info(self._h, C.byref(o)))
+        return o
+
+    def init_chains(self):
+        self._ck(self._lib.muca_batch_init_chains(self._h))
+
+    def set_weights(self, i, lnw):
+        a = np.ascontiguousarray(lnw, np.float64)
+        self._ck(self._lib.muca_batch_set_weights(self._h, i, a, a.size))
+
+    def get_weights(self, i):
+        L = self.instances[i][0]
+        a = np.zeros(L * L + 1)
+        self._ck(self._lib.muca_batch_get_weights(self._h, i, a, a.size))
+        return a
+
+    def histogram(self, i):
+        L = self.instances[i][0]
+        a = np.zeros(L * L + 1, np.uint64)
+        self._ck(self._lib.muca_batch_get_histogram(self._h, i, a, a.size))
+        return a
+
+    def run(self, starting_M=1, rule=UPDATE_TRIVIAL, nup_schedule=0, flat_minmean=0, max_iter=0, graph_iters=0,
+            reinit_chains=0, min_over_mean=0.0, d_kl_max=0.0, raise_on_not_converged=False):
+        """Returns (list of BatchResult, device seconds)."""
+        o = BatchRunOpts(starting_M=starting_M, rule=rule, nup_schedule=nup_schedule, flat_minmean=flat_minmean,
+                         max_iter=max_iter, graph_iters=graph_iters, reinit_chains=reinit_chains,
+                         min_over_mean=min_over_mean, d_kl_max=d_kl_max)
+        res = (BatchResult * len(self.instances))()
+        sec = C.c_double()
+        self._ck(self._lib.muca_batch_run(self._h, C.byref(o), res, C.byref(sec)),
+                 allow=() if raise_on_not_converged else (4,))
+        return list(res), sec.value

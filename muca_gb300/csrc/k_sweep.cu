@@ -36,479 +36,24 @@
 //   k_sweep_win   the same window core with the Philox numbers drawn by the
 //                 chain's own lane, one window ahead;
 //   k_sweep_generic  the reference step by step on the packed layout, any L.
-#include "muca_device.cuh"
-#include "muca_internal.h"
+#include "sweep_core.cuh"
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 namespace muca {
 
-template <int MODE>
-struct WeightType { using T = float; };
-template <>
-struct WeightType<kModeProduce> { using T = double; };
-
-__host__ __device__ constexpr size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
-
-// Shared-memory layout: weights | histogram (weight mode) | ring + barriers (specialised) | lattice.
-__host__ __device__ inline size_t smem_weights_bytes(int mode, uint32_t N)
-{
-    return align16((size_t)(N + 1) * (mode == kModeWeight ? 4 : 8));
-}
-__host__ __device__ inline size_t smem_hist_bytes(int mode, uint32_t N)
-{
-    return mode == kModeWeight ? align16((size_t)(N + 1) * 4) : 0;
-}
-// ring: [pair][depth][slot 0..7][lane 0..31] u32, then full/empty mbarriers
-__host__ __device__ inline size_t smem_ring_bytes(uint32_t pairs)
-{
-    return (size_t)pairs * kRingDepth * 8 * 32 * 4 + (size_t)pairs * kRingDepth * 2 * 8;
-}
-
-struct ChainState {
-    int E, EJ, M;
-};
-
-// A packed random word per attempt: bits 31..8 are the top 24 bits of the
-// acceptance draw r1 (all that u01fixedpt<float> uses: u = (1|(r1>>8))
-// 2^-24), bit 0 is the direction bit (u01fixedpt<float>(r3) < 0.5 <=>
-// r3 < 2^31, so the bit is r3's top bit, set for s -> s-1).
-__device__ __forceinline__ uint32_t pack_draw(uint32_t r1, uint32_t r3) { return (r1 & 0xFFFFFF00u) | (r3 >> 31); }
-
-template <int R>
-__device__ __forceinline__ void draw_group(uint32_t cc, uint32_t seed, uint32_t iter, const RoundKeys<R> &k1,
-                                           const RoundKeys<R> &k3, uint32_t *p)
-{
-    // one Philox block of the acceptance stream (k1) and one of the direction
-    // stream (k3) at the same counter (muca_delta_multigpu.cu:794-797)
-    const uint4 a = philox<R>(cc, seed, iter, kCtrTag, k1);
-    const uint4 b = philox<R>(cc, seed, iter, kCtrTag, k3);
-    p[0] = pack_draw(a.x, b.x);
-    p[1] = pack_draw(a.y, b.y);
-    p[2] = pack_draw(a.z, b.z);
-    p[3] = pack_draw(a.w, b.w);
-}
-
-// Histogram entry.  The u32 shared bins are drained into the u64 device
-// histogram by the lane whose increment finds 2^31 counts already there.
-template <int MODE>
-__device__ __forceinline__ void record(uint32_t *histS, unsigned long long *histG, int E, int M)
-{
-    if (MODE == kModeWeight) {
-        const uint32_t old = atomicAdd(&histS[E], 1u);
-        if (old >= 0x80000000u) {
-            const uint32_t v = atomicExch(&histS[E], 0u);
-            atomicAdd(&histG[E], (unsigned long long)v);
-        }
-    } else {
-        atomicAdd(&histG[(uint32_t)(M + E * E + 2 * E) >> 1], 1ull);
-    }
-}
-
-// Histogram entries of one window, merged into runs of equal bins per lane
-// (E_Delta moves by at most one per attempt, so a window's entries cluster).
-// `checked` (uniform: the launch can put 2^32 entries into one block's bins)
-// drains a u32 shared bin into the u64 device histogram once it holds 2^31.
-template <int MODE, int SLOTS>
-__device__ __forceinline__ void record_window(uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
-                                              const int (&Es)[SLOTS], const int (&Ms)[SLOTS], bool checked)
-{
-    if (MODE == kModeWeight) {
-        if (checked) {
-#pragma unroll
-            for (int t = 0; t < SLOTS; ++t) {
-                const uint32_t old = atomicAdd(&histS[Es[t]], 1u);
-                if (old >= 0x80000000u) atomicAdd(&histG[Es[t]], (unsigned long long)atomicExch(&histS[Es[t]], 0u));
-            }
-            return;
-        }
-        int cur = Es[0];
-        uint32_t cnt = 1;
-#pragma unroll
-        for (int t = 1; t < SLOTS; ++t) {
-            const bool same = Es[t] == cur;
-            if (!same) atomicAdd(&histS[cur], cnt);
-            cnt = same ? cnt + 1u : 1u;
-            cur = Es[t];
-        }
-        atomicAdd(&histS[cur], cnt);
-    } else {
-        uint32_t cur = (uint32_t)(Ms[0] + Es[0] * Es[0] + 2 * Es[0]) >> 1;
-        unsigned long long cnt = 1;
-#pragma unroll
-        for (int t = 1; t < SLOTS; ++t) {
-            const uint32_t b = (uint32_t)(Ms[t] + Es[t] * Es[t] + 2 * Es[t]) >> 1;
-            const bool same = b == cur;
-            if (!same) atomicAdd(&histG[cur], cnt);
-            cnt = same ? cnt + 1ull : 1ull;
-            cur = b;
-        }
-        atomicAdd(&histG[cur], cnt);
-    }
-}
-
-// One full window: the SLOTS same-parity (HALF) sites of word q of row `row`,
-// SLOTS consecutive attempts of the sweep, with packed draws p[].  lat points
-// at this lane's word 0 (stride cpb).  `store` is false for padding lanes:
-// they read another lane's spins, never accept (so their E stays at 2 and
-// every weight index E + dDel_t + dDel_t+1 stays in [0, 4]) and never write.
-template <int MODE, int SLOTS, int HALF>
-__device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
-                                            uint32_t row, uint32_t q, bool rec, bool store, bool checked,
-                                            const typename WeightType<MODE>::T *__restrict__ wS,
-                                            uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
-                                            ChainState &st, const uint32_t (&p)[SLOTS],
-                                            typename WeightType<MODE>::T eps)
-{
-    using WT = typename WeightType<MODE>::T;
-    constexpr uint32_t M2 = 0x33333333u, N1 = 0x11111111u;
-    const uint32_t rup = (row + 1 == L) ? 0u : row + 1;
-    const uint32_t rdn = (row == 0) ? L - 1 : row - 1;
-    uint32_t *pc = lat + (size_t)(row * WPR + q) * cpb;
-    const uint32_t C = *pc;
-    const uint32_t U = lat[(size_t)(rup * WPR + q) * cpb];
-    const uint32_t D = lat[(size_t)(rdn * WPR + q) * cpb];
-    // the one neighbour outside word q: left of the first even site, or
-    // right of the last odd site (wrapping along the row)
-    uint32_t sq, sb;
-    if (HALF == 0) {
-        sq = q ? q - 1 : (L - 1) >> 4;
-        sb = q ? 15u : ((L - 1) & 15u);
-    } else {
-        sq = (16 * q + 16 < L) ? q + 1 : 0u;
-        sb = 0u;
-    }
-    const uint32_t sv = spin_code(lat[(size_t)(row * WPR + sq) * cpb], sb);
-
-    // Nibble t of `ctr` holds the spin code (s+1) of the window's site t;
-    // nibble t of `nbs` the sum of its four neighbours' codes (0..8, no carries).
-    uint32_t ctr, nbs;
-    if (HALF == 0) {
-        const uint32_t oc = (C >> 2) & M2;  // odd sites: right neighbours, shifted: left ones
-        ctr = C & M2;
-        nbs = oc + ((oc << 4) | sv) + (U & M2) + (D & M2);
-    } else {
-        const uint32_t ec = C & M2;  // even sites: left neighbours, shifted: right ones
-        ctr = (C >> 2) & M2;
-        nbs = ec + ((ec >> 4) | (sv << (4 * (SLOTS - 1)))) + ((U >> 2) & M2) + ((D >> 2) & M2);
-    }
-    // Proposals of all sites at once, nibble-parallel:  s -> s +/- 1 with the
-    // cyclic wrap is code -> (code + 1 + d) mod 3, d the direction bit.
-    uint32_t dn = 0;
-#pragma unroll
-    for (int t = 0; t < SLOTS; ++t) dn |= (p[t] & 1u) << (4 * t);
-    const uint32_t x = ctr + N1 + dn;                              // 1..4
-    const uint32_t ge3 = ((x + N1) >> 2) & N1;                     // 1 where x >= 3
-    const uint32_t vnib = x - (ge3 + (ge3 << 1));                  // new codes 0..2
-    const uint32_t nzo = ((ctr ^ N1) | ((ctr ^ N1) >> 1)) & N1;    // s_old != 0
-    const uint32_t nzn = ((vnib ^ N1) | ((vnib ^ N1) >> 1)) & N1;  // s_new != 0
-    const uint32_t ddb = nzn + N1 - nzo;                           // dDel + 1 (0..2)
-    const uint32_t dvb = vnib + 0x22222222u - ctr;                 // s_new - s_old + 2 (0..4)
-
-    int dE[SLOTS], dDel[SLOTS], dM[SLOTS];
-    WT f2[SLOTS];
-    float lf[SLOTS];
-#pragma unroll
-    for (int t = 0; t < SLOTS; ++t) {
-        const int dv = (int)((dvb >> (4 * t)) & 7u) - 2;
-        dDel[t] = (int)((ddb >> (4 * t)) & 3u) - 1;
-        dE[t] = dv * (4 - (int)((nbs >> (4 * t)) & 15u));  // -(s_new - s_old) * (sum of neighbour spins)
-        dM[t] = dv;
-        f2[t] = (WT)(-2 * dE[t]);
-        lf[t] = __logf(u01f(p[t]));
-    }
-
-    // Sequential accept/reject over E_Delta:
-    //   accept  <=>  diff >= 0  ||  logf(u) < diff,
-    //   diff = (float)(-2 dE) + w[E + dDel] - w[E]   (muca_delta_multigpu.cu:810-816)
-    // decided with __logf(u) unless it lies within eps of diff in some lane;
-    // then the window is replayed with the exact logf(u).  The weight of the
-    // next attempt is fetched one attempt ahead for both outcomes (c0: this
-    // attempt rejected, c1: accepted), so no shared-memory load sits on the
-    // dependency chain from one decision to the next.
-    const ChainState s0 = st;
-    const WT wE0 = wS[st.E];
-    WT wE = wE0;
-    WT A = wS[st.E + dDel[0]];
-    WT c0 = A, c1 = A;
-    if (SLOTS > 1) {
-        c0 = wS[st.E + dDel[1]];
-        c1 = wS[st.E + dDel[0] + dDel[1]];
-    }
-    uint32_t accm = 0;
-    bool near = false;
-    int Es[SLOTS], Ms[SLOTS];
-#pragma unroll
-    for (int t = 0; t < SLOTS; ++t) {
-        WT diff;
-        if (MODE == kModeWeight)
-            diff = __fsub_rn(__fadd_rn((float)f2[t], (float)A), (float)wE);
-        else
-            diff = __dsub_rn(__dadd_rn((double)f2[t], (double)A), (double)wE);
-        const WT l = (WT)lf[t];
-        const bool acc = store && ((diff >= (WT)0) || (l < diff));
-        near |= (diff < (WT)0) && (fabs(l - diff) <= eps);
-        if (acc) {
-            st.E += dDel[t];
-            st.EJ += dE[t];
-            st.M += dM[t];
-            wE = A;
-            accm |= 0xFu << (4 * t);
-        }
-        Es[t] = st.E;
-        Ms[t] = st.M;
-        if (t + 1 < SLOTS) {
-            A = acc ? c1 : c0;
-            if (t + 2 < SLOTS) {
-                c0 = wS[st.E + dDel[t + 2]];
-                c1 = wS[st.E + dDel[t + 1] + dDel[t + 2]];
-            }
-        }
-    }
-    if (__any_sync(0xffffffffu, near)) {
-        st = s0;
-        wE = wE0;
-        accm = 0;
-#pragma unroll
-        for (int t = 0; t < SLOTS; ++t) {
-            const WT wn = wS[st.E + dDel[t]];
-            WT diff;
-            if (MODE == kModeWeight)
-                diff = __fsub_rn(__fadd_rn((float)f2[t], (float)wn), (float)wE);
-            else
-                diff = __dsub_rn(__dadd_rn((double)f2[t], (double)wn), (double)wE);
-            bool acc = diff >= (WT)0;
-            if (!acc) acc = (WT)logf(u01f(p[t])) < diff;
-            acc = acc && store;
-            if (acc) {
-                st.E += dDel[t];
-                st.EJ += dE[t];
-                st.M += dM[t];
-                wE = wn;
-                accm |= 0xFu << (4 * t);
-            }
-            Es[t] = st.E;
-            Ms[t] = st.M;
-        }
-    }
-    const uint32_t merged = (ctr & ~accm) | (vnib & accm);
-    if (store) *pc = (HALF == 0) ? ((C & ~M2) | merged) : ((C & M2) | (merged << 2));
-    if (rec) record_window<MODE, SLOTS>(histS, histG, Es, Ms, checked);
-}
-
-// The first `len` (< window size) attempts of a window, one at a time as
-// the reference writes them; only the last window of a phase is partial.
-template <int MODE>
-__device__ __noinline__ void partial_core(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
-                                          uint32_t row, uint32_t q, uint32_t half, uint32_t len, bool rec,
-                                          bool store, const typename WeightType<MODE>::T *__restrict__ wS,
-                                          uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
-                                          ChainState &st, const uint32_t *p)
-{
-    using WT = typename WeightType<MODE>::T;
-    const uint32_t rup = (row + 1 == L) ? 0u : row + 1;
-    const uint32_t rdn = (row == 0) ? L - 1 : row - 1;
-    for (uint32_t t = 0; t < len; ++t) {
-        const uint32_t col = 16u * q + 2u * t + half;
-        const uint32_t cl = col ? col - 1 : L - 1, cr = (col + 1 == L) ? 0u : col + 1;
-        uint32_t *pw = lat + (size_t)(row * WPR + (col >> 4)) * cpb;
-        const int os = (int)spin_code(*pw, col) - 1;
-        int ns = os + ((p[t] & 1u) ? -1 : 1);
-        ns = ns - 3 * (ns == 2) + 3 * (ns == -2);
-        const int nb = (int)spin_code(lat[(size_t)(row * WPR + (cl >> 4)) * cpb], cl) +
-                       (int)spin_code(lat[(size_t)(row * WPR + (cr >> 4)) * cpb], cr) +
-                       (int)spin_code(lat[(size_t)(rup * WPR + (col >> 4)) * cpb], col) +
-                       (int)spin_code(lat[(size_t)(rdn * WPR + (col >> 4)) * cpb], col) - 4;
-        const int dE = -(ns - os) * nb, dDel = ns * ns - os * os, dM = ns - os;
-        WT diff;
-        if (MODE == kModeWeight)
-            diff = __fsub_rn(__fadd_rn((float)(-2 * dE), (float)wS[st.E + dDel]), (float)wS[st.E]);
-        else
-            diff = __dsub_rn(__dadd_rn((double)(-2 * dE), (double)wS[st.E + dDel]), (double)wS[st.E]);
-        bool acc = diff >= (WT)0;
-        if (!acc) acc = (WT)logf(u01f(p[t])) < diff;
-        if (acc && store) {
-            const uint32_t sh = 2u * (col & 15u);
-            *pw = (*pw & ~(3u << sh)) | ((uint32_t)(ns + 1) << sh);
-            st.E += dDel;
-            st.EJ += dE;
-            st.M += dM;
-        }
-        if (rec) record<MODE>(histS, histG, st.E, st.M);
-    }
-}
-
-// Stage weights, clear the histogram, stage this block's lattice; returns
-// the lane's lattice base (shared or global).  Only lanes < cpb copy.
-template <int MODE, bool LAT_SMEM>
-__device__ __forceinline__ uint32_t *prologue(const SweepArgs &a, unsigned char *smem, size_t lat_offset,
-                                              uint32_t cpb, uint32_t lane, typename WeightType<MODE>::T *&wS,
-                                              uint32_t *&histS, uint32_t *&gl)
-{
-    using WT = typename WeightType<MODE>::T;
-    const uint32_t N = a.N, nt = blockDim.x, tid = threadIdx.x;
-    wS = reinterpret_cast<WT *>(smem);
-    histS = reinterpret_cast<uint32_t *>(smem + smem_weights_bytes(MODE, N));
-    uint32_t *latS = reinterpret_cast<uint32_t *>(smem + lat_offset);
-    const WT *wg = reinterpret_cast<const WT *>(a.w);
-    for (uint32_t i = tid; i <= N; i += nt) wS[i] = wg[i];
-    if (MODE == kModeWeight)
-        for (uint32_t i = tid; i <= N; i += nt) histS[i] = 0u;
-    const uint32_t words = a.L * a.WPR;
-    const uint32_t l = lane < cpb ? lane : 0u;  // padding lanes read lane 0's words, never write
-    gl = a.lat + (size_t)blockIdx.x * words * cpb + l;
-    if (LAT_SMEM) {
-        if (lane < cpb)
-            for (uint32_t w = 0; w < words; ++w) latS[(size_t)w * cpb + lane] = gl[(size_t)w * cpb];
-        return latS + l;
-    }
-    return gl;
-}
-
-template <int MODE>
-__device__ __forceinline__ void drain_hist(uint32_t *histS, unsigned long long *histG, uint32_t N)
-{
-    if (MODE == kModeWeight) {
-        for (uint32_t b = threadIdx.x; b <= N; b += blockDim.x) {
-            const uint32_t v = histS[b];
-            if (v) atomicAdd(&histG[b], (unsigned long long)v);
-        }
-    }
-}
-
-// Walks the window sequence of a launch: phase 0 (therm) then phase 1 (nup),
-// each starting at site 0 of the sweep; calls f(row, q, half, cnt, len, rec)
-// and stops early when f returns false.
-template <typename F>
-__device__ __forceinline__ void for_each_window(uint32_t L, uint32_t WPR, unsigned long long therm,
-                                                unsigned long long nup, F &&f)
-{
-    for (int phase = 0; phase < 2; ++phase) {
-        const unsigned long long n = phase ? nup : therm;
-        unsigned long long i = 0;
-        uint32_t row = 0, q = 0, half = 0;
-        while (i < n) {
-            const uint32_t cnt = (min(16u * q + 16u, L) - 16u * q) >> 1;
-            const uint32_t len = (n - i < cnt) ? (uint32_t)(n - i) : cnt;
-            if (!f(row, q, half, cnt, len, phase == 1)) return;
-            i += len;
-            if (++q == WPR) {
-                q = 0;
-                if (++row == L) { row = 0; half ^= 1u; }
-            }
-        }
-    }
-}
-
-template <int MODE, int R>
-struct ChainSetup {
-    uint32_t chain, seed;
-    bool active;
-    RoundKeys<R> k1, k3;
-    __device__ __forceinline__ void init(const SweepArgs &a, uint32_t cpb, uint32_t lane)
-    {
-        chain = blockIdx.x * cpb + lane;
-        active = lane < cpb && chain < a.nchains;
-        const uint32_t dev = chain / a.chains_per_dev;
-        const uint32_t W = chain - dev * a.chains_per_dev;
-        seed = a.seed_base + a.seed_dev_mul * dev;
-        k1.init(a.k1_mul * W + a.k1_add, a.k1_hi);
-        k3.init(a.k3_mul * W + a.k3_add, a.k3_hi);
-    }
-};
-
-__device__ __forceinline__ bool launch_params(const SweepArgs &a, uint32_t &iter, unsigned long long &nup)
-{
-    iter = a.iter;
-    nup = a.nup;
-    if (a.dyn) {
-        if (a.dyn[2]) return false;
-        iter = a.dyn[0];
-        nup = a.dyn[1];
-    }
-    return true;
-}
-
 // ---------------------------------------------------------------------------
-// Windowed kernel: every lane draws its own Philox numbers one window ahead
-// (`next` holds the packed draws of the next two groups, counters cc-1, cc).
-// blockDim = cpb rounded up to a warp; lanes >= cpb are padding.
+// Windowed kernel: one block per chain block, blockDim = cpb rounded up to a warp.
 template <int MODE, int R, bool LAT_SMEM>
 __global__ void __launch_bounds__(256, 1) k_sweep_win(const SweepArgs a, uint32_t cpb)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    using WT = typename WeightType<MODE>::T;
     uint32_t iter;
     unsigned long long nup;
     if (!launch_params(a, iter, nup)) return;
-    const uint32_t lane = threadIdx.x;
-    WT *wS;
-    uint32_t *histS, *gl;
-    const size_t lat_off = smem_weights_bytes(MODE, a.N) + smem_hist_bytes(MODE, a.N);
-    uint32_t *lat = prologue<MODE, LAT_SMEM>(a, smem, lat_off, cpb, lane, wS, histS, gl);
-    __syncthreads();
-    ChainSetup<MODE, R> cs;
-    cs.init(a, cpb, lane);
-    const bool store = lane < cpb;
-    ChainState st;
-    st.E = cs.active ? a.edel[cs.chain] : (store ? 0 : 2);
-    st.EJ = cs.active ? a.ej[cs.chain] : 0;
-    st.M = (cs.active && MODE == kModeProduce) ? a.mag[cs.chain] : 0;
-    const WT eps = (WT)a.log_eps;
-    // u32 shared bins can overflow only if the launch can record 2^32 entries in one block
-    const bool checked = (unsigned long long)cpb * nup >= 0xFFFFFFFFull;
-    const uint32_t L = a.L, WPR = a.WPR;
-    uint32_t next[8];
-    draw_group<R>(1u, cs.seed, iter, cs.k1, cs.k3, next);
-    draw_group<R>(2u, cs.seed, iter, cs.k1, cs.k3, next + 4);
-    uint32_t cc = 2;
-    auto advance = [&](uint32_t groups) {
-        if (groups == 2) {
-            draw_group<R>(cc + 1, cs.seed, iter, cs.k1, cs.k3, next);
-            draw_group<R>(cc + 2, cs.seed, iter, cs.k1, cs.k3, next + 4);
-            cc += 2;
-        } else {
-#pragma unroll
-            for (int t = 0; t < 4; ++t) next[t] = next[t + 4];
-            draw_group<R>(cc + 1, cs.seed, iter, cs.k1, cs.k3, next + 4);
-            cc += 1;
-        }
-    };
-    for_each_window(L, WPR, a.therm, nup, [&](uint32_t row, uint32_t q, uint32_t half, uint32_t cnt, uint32_t len,
-                                              bool rec_phase) {
-        const bool rec = rec_phase && cs.active;
-        if (len < cnt) {
-            partial_core<MODE>(lat, cpb, L, WPR, row, q, half, len, rec, store, wS, histS, a.hist, st, next);
-            advance((len + 3u) >> 2);
-        } else if (cnt == 8) {
-            uint32_t p[8];
-#pragma unroll
-            for (int t = 0; t < 8; ++t) p[t] = next[t];
-            advance(2);  // independent of the window below: overlaps its scan
-            if (half) window_core<MODE, 8, 1>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps);
-            else      window_core<MODE, 8, 0>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps);
-        } else {
-            uint32_t p[4];
-#pragma unroll
-            for (int t = 0; t < 4; ++t) p[t] = next[t];
-            advance(1);
-            if (half) window_core<MODE, 4, 1>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps);
-            else      window_core<MODE, 4, 0>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps);
-        }
-        return true;
-    });
-    if (LAT_SMEM && store) {
-        const uint32_t words = L * WPR;
-        for (uint32_t w = 0; w < words; ++w) gl[(size_t)w * cpb] = lat[(size_t)w * cpb];
-    }
-    if (cs.active) {
-        a.edel[cs.chain] = st.E;
-        a.ej[cs.chain] = st.EJ;
-        if (MODE == kModeProduce) a.mag[cs.chain] = st.M;
-    }
-    __syncthreads();
-    drain_hist<MODE>(histS, a.hist, a.N);
+    win_sweep_block<MODE, R, LAT_SMEM>(a, smem, cpb, blockIdx.x, iter, nup);
 }
 
 // ---------------------------------------------------------------------------
@@ -569,10 +114,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
     WT *wS;
     uint32_t *histS, *gl;
     const size_t lat_off = ring_off + smem_ring_bytes(P);
-    uint32_t *lat = prologue<MODE, LAT_SMEM>(a, smem, lat_off, cpb, producer ? 0xFFFFFFFFu : lane, wS, histS, gl);
+    uint32_t *lat = prologue<MODE, LAT_SMEM>(a, smem, lat_off, cpb, producer ? 0xFFFFFFFFu : lane, blockIdx.x, wS, histS, gl);
     __syncthreads();
     ChainSetup<MODE, R> cs;
-    cs.init(a, cpb, lane);
+    cs.init(a, cpb, lane, blockIdx.x);
     const uint32_t L = a.L, WPR = a.WPR;
     const long long deadline = clock64() + kWaitCycles;
     uint32_t w = 0;  // window counter (ring position)
@@ -662,10 +207,10 @@ __global__ void __launch_bounds__(256) k_sweep_generic(const SweepArgs a, uint32
     WT *wS;
     uint32_t *histS, *gl;
     const size_t lat_off = smem_weights_bytes(MODE, a.N) + smem_hist_bytes(MODE, a.N);
-    uint32_t *lat = prologue<MODE, LAT_SMEM>(a, smem, lat_off, cpb, lane, wS, histS, gl);
+    uint32_t *lat = prologue<MODE, LAT_SMEM>(a, smem, lat_off, cpb, lane, blockIdx.x, wS, histS, gl);
     __syncthreads();
     ChainSetup<MODE, R> cs;
-    cs.init(a, cpb, lane);
+    cs.init(a, cpb, lane, blockIdx.x);
     const bool store = lane < cpb;
     int E = cs.active ? a.edel[cs.chain] : 0;
     int EJ = cs.active ? a.ej[cs.chain] : 0;
@@ -769,6 +314,23 @@ cudaError_t measure_logf_bracket(float *max_abs_err, cudaStream_t s)
     std::memcpy(&f, &h, sizeof f);
     *max_abs_err = f;
     return e;
+}
+
+cudaError_t device_log_eps(int device, cudaStream_t s, double *eps)
+{
+    static std::mutex mu;
+    static float maxerr[64];
+    static bool have[64];
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!have[device]) {
+        const cudaError_t e = measure_logf_bracket(&maxerr[device], s);
+        if (e != cudaSuccess) return e;
+        have[device] = true;
+    }
+    const float m = maxerr[device];
+    *eps = (m >= 0.0f && m < 1e-2f) ? 2.0 * (double)m + 1e-30 : 1e30;
+    return cudaSuccess;
 }
 
 // ---------------------------------------------------------------------------

@@ -47,13 +47,13 @@ struct AddD { __device__ double operator()(double a, double b) const { return a 
 // Statistics of hist[0..N], then (if the update is due) the weight update.
 // ctl == nullptr: standalone call, update iff rule >= 0.
 // ctl != nullptr: one iteration of a device-driven run (see RunCtl).
-__global__ void __launch_bounds__(kUpdThreads) k_weight_update(const unsigned long long *__restrict__ hist, uint32_t N,
-                                                                double *__restrict__ lnw, float *__restrict__ w32,
-                                                                double *__restrict__ p_acc, int rule,
-                                                                HistStatsDev *__restrict__ stats,
-                                                                RunCtl *__restrict__ ctl)
+// `dyn`: dynamic shared memory of update_smem(N, rule) bytes.
+__device__ __forceinline__ void weight_update_body(const unsigned long long *__restrict__ hist, uint32_t N,
+                                                   double *__restrict__ lnw, float *__restrict__ w32,
+                                                   double *__restrict__ p_acc, int rule,
+                                                   HistStatsDev *__restrict__ stats, RunCtl *__restrict__ ctl,
+                                                   unsigned char *dyn)
 {
-    extern __shared__ __align__(16) unsigned char dyn[];
     __shared__ int shi[32];
     __shared__ unsigned long long shu[32];
     __shared__ double shd[32];
@@ -202,6 +202,27 @@ __global__ void __launch_bounds__(kUpdThreads) k_weight_update(const unsigned lo
     }
 }
 
+__global__ void __launch_bounds__(kUpdThreads) k_weight_update(const unsigned long long *__restrict__ hist, uint32_t N,
+                                                                double *__restrict__ lnw, float *__restrict__ w32,
+                                                                double *__restrict__ p_acc, int rule,
+                                                                HistStatsDev *__restrict__ stats,
+                                                                RunCtl *__restrict__ ctl)
+{
+    extern __shared__ __align__(16) unsigned char dyn[];
+    weight_update_body(hist, N, lnw, w32, p_acc, rule, stats, ctl, dyn);
+}
+
+// One iteration's tail for every instance of a batch (block i = instance i),
+// then the count of instances that are still running.
+__global__ void __launch_bounds__(kUpdThreads) k_batch_update(const BatchInst *__restrict__ insts,
+                                                               uint32_t *__restrict__ running)
+{
+    extern __shared__ __align__(16) unsigned char dyn[];
+    const BatchInst &I = insts[blockIdx.x];
+    weight_update_body(I.a.hist, I.a.N, I.lnw, I.w32, I.p_acc, (int)I.rule, nullptr, I.ctl, dyn);
+    if (threadIdx.x == 0 && !I.ctl->st.stop) atomicAdd(running, 1u);
+}
+
 __global__ void k_run_clear(unsigned long long *hist, uint32_t n, const RunCtl *ctl)
 {
     if (ctl->st.stop) return;
@@ -238,6 +259,22 @@ cudaError_t launch_run_update(const unsigned long long *hist, double *lnw, float
     cudaError_t e = prep_update(N, rule);
     if (e != cudaSuccess) return e;
     k_weight_update<<<1, kUpdThreads, update_smem(N, rule), s>>>(hist, N, lnw, w32, p_acc, rule, nullptr, ctl);
+    return cudaGetLastError();
+}
+
+cudaError_t prepare_batch_update(uint32_t max_N, int any_recursion)
+{
+    const size_t dyn = any_recursion ? update_smem(max_N, 2) : 0;
+    if (dyn > 48 * 1024)
+        return cudaFuncSetAttribute(k_batch_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    return cudaSuccess;
+}
+
+cudaError_t launch_batch_update(const BatchInst *insts, uint32_t n_inst, uint32_t max_N, int any_recursion,
+                                uint32_t *running, cudaStream_t s)
+{
+    const size_t dyn = any_recursion ? update_smem(max_N, 2) : 0;
+    k_batch_update<<<n_inst, kUpdThreads, dyn, s>>>(insts, running);
     return cudaGetLastError();
 }
 

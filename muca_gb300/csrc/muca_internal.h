@@ -58,6 +58,10 @@ constexpr uint32_t kRingDepth = 4;  // windows the producer warps may run ahead
 SweepPlan plan_sweep(int mode, int rounds, uint32_t L, uint32_t nchains, size_t smem_optin, int sms, int kernel = -1);
 // Worst case of |__logf(u) - logf(u)| over u = (2k+1) 2^-24, k < 2^23 (exhaustive, on the device).
 cudaError_t measure_logf_bracket(float *max_abs_err, cudaStream_t s);
+// The bound of the fast acceptance test for `device` (current): twice the
+// measured worst case, measured once per device and cached; 1e30 (every
+// decision on the exact logf) if the measurement is implausible.
+cudaError_t device_log_eps(int device, cudaStream_t s, double *eps);
 cudaError_t launch_sweep(const SweepPlan &p, const SweepArgs &a, cudaStream_t s);
 
 // Lattice helpers (k_lattice.cu).
@@ -116,6 +120,42 @@ struct RunCtl {
     double mom_thr, dkl_max;
     IterRecordDev *recs;
 };
+// One instance of a batch of weight runs: its sweep arguments (a.dyn points
+// at ctl->st, a.w at w32), its run state and its FP64 weights.  btab[dE + 8]
+// = (float)(-beta * dE) for dE = -8..8, the Metropolis term of any beta.
+struct BatchInst {
+    SweepArgs a;
+    RunCtl *ctl;
+    double *lnw, *p_acc;
+    float *w32;
+    float btab[17];
+    uint32_t rule;
+};
+// A unit of sweep work: chain block `blk` of instance `inst`.
+struct BatchItem {
+    uint32_t inst, blk;
+};
+// Clears the histograms of the running instances and resets the work counter.
+cudaError_t launch_batch_prep(const BatchInst *insts, uint32_t n_inst, uint32_t *next_item, uint32_t *running,
+                              cudaStream_t s);
+// Persistent sweep over `items` (fetched through *next_item) with chain
+// blocks of cpb chains; lat_smem / hist_smem select the shared-memory
+// placement.  grid blocks of roundup32(cpb) threads and `smem` bytes.
+cudaError_t launch_batch_sweep(const BatchInst *insts, const BatchItem *items, uint32_t n_items, uint32_t *next_item,
+                               uint32_t cpb, int rounds, bool lat_smem, bool hist_smem, uint32_t grid, size_t smem,
+                               cudaStream_t s);
+// Dynamic shared memory of one batch sweep block for an instance of size L.
+size_t batch_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem, bool hist_smem);
+// Blocks of the batch sweep that fit on one SM with `smem` bytes each; also
+// sets the kernel's shared-memory limit to `smem` (call before any capture).
+// The launch with that shape needs no further attribute call.
+cudaError_t batch_sweep_occupancy(uint32_t cpb, int rounds, bool lat_smem, bool hist_smem, size_t smem, int *blocks);
+// Sets the update kernel's shared-memory limit (call before any capture).
+cudaError_t prepare_batch_update(uint32_t max_N, int any_recursion);
+// The update step of every instance; *running += instances not stopped.
+cudaError_t launch_batch_update(const BatchInst *insts, uint32_t n_inst, uint32_t max_N, int any_recursion,
+                                uint32_t *running, cudaStream_t s);
+
 // One iteration's tail: statistics, width/convergence bookkeeping, weight
 // update, schedule of the next NUPDATES; a no-op once st.stop is set.
 cudaError_t launch_run_update(const unsigned long long *hist, double *lnw, float *w32, double *p_acc,

@@ -182,6 +182,21 @@ static inline float accept_logf(uint32_t r)
     return g_logf_tab ? g_logf_tab[r >> 9] : logf(orc_u01fixedpt_f32(r));
 }
 
+/* Metropolis term of the weight sweep.  The reference fixes beta = 2 and
+ * forms -dE*2 as an int (muca_delta_multigpu.cu:810); orc_set_beta(b > 0)
+ * uses the FP32 value (float)(-(b * dE)) instead, as the batched engine does
+ * for any beta (for b = 2 the two are the same float). */
+static int g_beta_on = 0;
+static float g_btab[17];
+
+void orc_set_beta(double beta)
+{
+    g_beta_on = beta > 0.0;
+    for (int d = -8; d <= 8; ++d) g_btab[d + 8] = (float)(-(beta * (double)d));
+}
+
+static inline float beta_term(int dE) { return g_beta_on ? g_btab[dE + 8] : (float)(-dE * 2); }
+
 /* Kernel mcs of muca_delta_multigpu.cu:737-829 for one chain. */
 static void weight_chain(unsigned L, const uint32_t *nv, const uint32_t *ix, unsigned W, int8_t *s,
                          int32_t *ej, int32_t *edel, const float *w, uint64_t *hist,
@@ -204,7 +219,7 @@ static void weight_chain(unsigned L, const uint32_t *nv, const uint32_t *ix, uns
             unsigned idx = ix[i % N];
             int os, ns, dE, dDel;
             propose(s, nv, idx, r3[i % 4], &os, &ns, &dE, &dDel);
-            float diff = -dE * 2 + w[E + dDel] - w[E];
+            float diff = beta_term(dE) + w[E + dDel] - w[E];
             if (diff >= 0) {
                 s[idx] = (int8_t)ns; energy += dE; E += dDel;
             } else if (accept_logf(r1[i % 4]) < diff) {

@@ -65,6 +65,10 @@ void orc_set_logf_table(const float *tab);
 /* the same table with libm's logf (2^23 floats), to check the lookup */
 void orc_libm_logf_table(float *tab);
 
+/* beta of orc_weight_sweep: 0 = the reference's literal -dE*2; b > 0 =
+ * the FP32 term (float)(-(b*dE)) of the batched engine. */
+void orc_set_beta(double beta);
+
 /* ---- sweeps ----
  * orc_weight_sweep: muca_delta_multigpu.cu:737-829 (kernel mcs), FP32 weights,
  * histogram of E_Delta after every production attempt (added to hist, u64).

@@ -100,6 +100,7 @@ def lib():
     L.orc_weight_run.restype = C.c_uint
     L.orc_set_logf_table.argtypes = [C.c_void_p]
     L.orc_libm_logf_table.argtypes = [_f32p]
+    L.orc_set_beta.argtypes = [C.c_double]
     _LIB = L
     return L
 
