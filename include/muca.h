@@ -120,11 +120,13 @@ typedef struct muca_run_opts {
     uint32_t max_iter;      /* iteration cap (0 = 1000000) */
     uint32_t init_scheme;   /* muca_init_scheme for the chains; MUCA_INIT_WEIGHT for parity */
     uint32_t reinit_chains; /* 1: initialise chains at the start (the reference does, :340-354) */
-    uint32_t nup_schedule;  /* 0: reference ((NUP+1)*1.01 once width==N, :379-382); 1: doubling */
+    uint32_t nup_schedule;  /* 0: reference ((NUP+1)*1.01 once width==N, :379-382); 1: doubling once
+                               width==N; 2: doubling every iteration from the first (cap 2^30) */
     double min_over_mean;   /* threshold for flat_minmean (0 = 0.5) */
     double d_kl_max;        /* threshold of the D_KL test (0 = 1e-4) */
     uint32_t width_start;   /* initial running width (0 = 10, :314); the reference keeps the
                                previous jack's width for jack > 0 */
+    uint32_t nup_max;       /* cap of NUPDATES (0: none for schedule 0, 2^30 for the doubling ones) */
 } muca_run_opts;
 
 typedef struct muca_iter_record {
@@ -294,14 +296,18 @@ typedef struct muca_batch_info {
 typedef struct muca_batch_run_opts {
     uint32_t starting_M;    /* initial NUPDATES of every instance */
     uint32_t rule;          /* muca_update_rule */
-    uint32_t nup_schedule;  /* 0: (NUP+1)*1.01 once width == N (:379-382); 1: doubling */
+    uint32_t nup_schedule;  /* 0: (NUP+1)*1.01 once width == N (:379-382); 1: doubling once width == N;
+                               2: doubling every iteration (cap 2^30) */
     uint32_t flat_minmean;  /* 0: stop at width == N && D_KL < d_kl_max; 1: at min/mean >= min_over_mean */
     uint32_t max_iter;      /* per instance (0 = 1000000) */
     uint32_t graph_iters;   /* iterations per captured graph (0 = 16) */
     uint32_t reinit_chains; /* 1: initial spins again before the run */
-    uint32_t reserved;
+    uint32_t nup_max;       /* cap of NUPDATES (0: none for schedule 0, 2^30 for the doubling ones) */
     double min_over_mean;   /* 0 = 0.5 */
     double d_kl_max;        /* 0 = 1e-4 */
+    uint32_t starting_sweeps; /* nonzero: instance i starts at NUPDATES = starting_sweeps * N_i
+                                 (replaces starting_M) */
+    uint32_t reserved;
 } muca_batch_run_opts;
 
 typedef struct muca_batch_result {

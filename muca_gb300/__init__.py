@@ -71,7 +71,8 @@ class RunOpts(C.Structure):
     _fields_ = [("jack", C.c_uint32), ("starting_M", C.c_uint32), ("therm", C.c_uint32), ("rule", C.c_uint32),
                 ("hold_until_full", C.c_uint32), ("flat_minmean", C.c_uint32), ("max_iter", C.c_uint32),
                 ("init_scheme", C.c_uint32), ("reinit_chains", C.c_uint32), ("nup_schedule", C.c_uint32),
-                ("min_over_mean", C.c_double), ("d_kl_max", C.c_double), ("width_start", C.c_uint32)]
+                ("min_over_mean", C.c_double), ("d_kl_max", C.c_double), ("width_start", C.c_uint32),
+                ("nup_max", C.c_uint32)]
 
 
 class IterRecord(C.Structure):
@@ -117,8 +118,8 @@ class BatchInfo(C.Structure):
 class BatchRunOpts(C.Structure):
     _fields_ = [("starting_M", C.c_uint32), ("rule", C.c_uint32), ("nup_schedule", C.c_uint32),
                 ("flat_minmean", C.c_uint32), ("max_iter", C.c_uint32), ("graph_iters", C.c_uint32),
-                ("reinit_chains", C.c_uint32), ("reserved", C.c_uint32), ("min_over_mean", C.c_double),
-                ("d_kl_max", C.c_double)]
+                ("reinit_chains", C.c_uint32), ("nup_max", C.c_uint32), ("min_over_mean", C.c_double),
+                ("d_kl_max", C.c_double), ("starting_sweeps", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class BatchResult(C.Structure):
@@ -323,11 +324,12 @@ class Engine:
 
     def weight_run(self, starting_M=1, jack=0, rule=UPDATE_TRIVIAL, hold_until_full=0, flat_minmean=0,
                    max_iter=0, therm=0, init_scheme=INIT_WEIGHT, reinit_chains=1, nup_schedule=0,
-                   min_over_mean=0.0, d_kl_max=0.0, width_start=0, records=1000, raise_on_not_converged=False):
+                   min_over_mean=0.0, d_kl_max=0.0, width_start=0, nup_max=0, records=1000,
+                   raise_on_not_converged=False):
         o = RunOpts(jack=jack, starting_M=starting_M, therm=therm, rule=rule, hold_until_full=hold_until_full,
                     flat_minmean=flat_minmean, max_iter=max_iter, init_scheme=init_scheme,
                     reinit_chains=reinit_chains, nup_schedule=nup_schedule, min_over_mean=min_over_mean,
-                    d_kl_max=d_kl_max, width_start=width_start)
+                    d_kl_max=d_kl_max, width_start=width_start, nup_max=nup_max)
         res = RunResult()
         recs = (IterRecord * max(records, 1))()
         st = self._lib.muca_weight_run(self._h, C.byref(o), C.byref(res), recs, records)
@@ -426,11 +428,12 @@ class Batch:
         return a
 
     def run(self, starting_M=1, rule=UPDATE_TRIVIAL, nup_schedule=0, flat_minmean=0, max_iter=0, graph_iters=0,
-            reinit_chains=0, min_over_mean=0.0, d_kl_max=0.0, raise_on_not_converged=False):
+            reinit_chains=0, min_over_mean=0.0, d_kl_max=0.0, nup_max=0, starting_sweeps=0,
+            raise_on_not_converged=False):
         """Returns (list of BatchResult, device seconds)."""
         o = BatchRunOpts(starting_M=starting_M, rule=rule, nup_schedule=nup_schedule, flat_minmean=flat_minmean,
-                         max_iter=max_iter, graph_iters=graph_iters, reinit_chains=reinit_chains,
-                         min_over_mean=min_over_mean, d_kl_max=d_kl_max)
+                         max_iter=max_iter, graph_iters=graph_iters, reinit_chains=reinit_chains, nup_max=nup_max,
+                         min_over_mean=min_over_mean, d_kl_max=d_kl_max, starting_sweeps=starting_sweeps)
         res = (BatchResult * len(self.instances))()
         sec = C.c_double()
         self._ck(self._lib.muca_batch_run(self._h, C.byref(o), res, C.byref(sec)),

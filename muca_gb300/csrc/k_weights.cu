@@ -47,6 +47,24 @@ struct AddD { __device__ double operator()(double a, double b) const { return a 
 // Statistics of hist[0..N], then (if the update is due) the weight update.
 // ctl == nullptr: standalone call, update iff rule >= 0.
 // ctl != nullptr: one iteration of a device-driven run (see RunCtl).
+// NUPDATES of the next iteration.  sched 0: the reference's (NUP+1)*1.01
+// once the width is full (muca_delta_multigpu.cu:379-382); 1: doubling once
+// the width is full; 2: doubling every iteration.  The result is capped at
+// `cap` (0: no cap for sched 0, 2^30 for doubling) but never falls below nup.
+__host__ __device__ __forceinline__ uint32_t next_nupdates(uint32_t nup, bool full, uint32_t sched, uint32_t cap)
+{
+    unsigned long long nx = nup;
+    if (sched == 2 || (sched == 1 && full)) {
+        nx = 2ull * nup;
+        if (cap == 0) cap = 1u << 30;
+    } else if (sched == 0 && full) {
+        const unsigned nu = nup + 1u;
+        nx = (unsigned)(nu * 1.01);
+    }
+    if (cap != 0 && nx > cap) nx = cap > nup ? cap : nup;
+    return (uint32_t)nx;
+}
+
 // `dyn`: dynamic shared memory of update_smem(N, rule) bytes.
 __device__ __forceinline__ void weight_update_body(const unsigned long long *__restrict__ hist, uint32_t N,
                                                    double *__restrict__ lnw, float *__restrict__ w32,
@@ -129,14 +147,7 @@ __device__ __forceinline__ void weight_update_body(const unsigned long long *__r
                 if (st.k >= ctl->max_iter) {
                     st.stop = 1;
                 } else {
-                    if (st.width == N) {
-                        if (ctl->sched == 0) {
-                            unsigned nu = st.nup + 1u;           // :380-381
-                            st.nup = (unsigned)(nu * 1.01);
-                        } else {
-                            st.nup = st.nup * 2u;
-                        }
-                    }
+                    st.nup = next_nupdates(st.nup, st.width == N, ctl->sched, ctl->nup_max);
                     st.total_run += (unsigned long long)st.nup * ctl->nchains_total;
                 }
             }

@@ -528,6 +528,7 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "weight run needs a weight-mode context");
     if (o->rule > MUCA_UPDATE_RECURSION) return fail(c, MUCA_ERR_BAD_ARG, "rule %u", o->rule);
     if (o->starting_M == 0) return fail(c, MUCA_ERR_BAD_ARG, "starting_M must be >= 1");
+    if (o->nup_schedule > 2) return fail(c, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..2)", o->nup_schedule);
     CUDA_TRY(c, cudaSetDevice(c->device));
     const auto t0 = std::chrono::steady_clock::now();
     if (o->reinit_chains) {
@@ -549,7 +550,12 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     // the schedule runs at the top of every iteration (:379-382), so a run that
     // starts at full width (a later jack) grows NUPDATES before its first sweep;
     // the device applies it between iterations from then on
-    if (h.st.width == c->N) h.st.nup = o->nup_schedule ? h.st.nup * 2u : (unsigned)((h.st.nup + 1u) * 1.01);
+    if (h.st.width == c->N && o->nup_schedule != 2) {
+        unsigned long long nx = o->nup_schedule ? 2ull * h.st.nup : (unsigned)((h.st.nup + 1u) * 1.01);
+        const uint32_t cap = o->nup_max ? o->nup_max : (o->nup_schedule ? (1u << 30) : 0u);
+        if (cap != 0 && nx > cap) nx = cap > h.st.nup ? cap : h.st.nup;
+        h.st.nup = (uint32_t)nx;
+    }
     h.st.total_run = (unsigned long long)h.st.nup * c->nchains;
     h.N = c->N;
     h.nchains_total = c->nchains;
@@ -558,6 +564,7 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     h.flat_minmean = o->flat_minmean;
     h.max_iter = max_iter;
     h.sched = o->nup_schedule;
+    h.nup_max = o->nup_max;
     h.mom_thr = o->min_over_mean > 0 ? o->min_over_mean : 0.5;
     h.dkl_max = o->d_kl_max > 0 ? o->d_kl_max : 1e-4;
     h.recs = need ? c->d_recs : nullptr;

@@ -257,7 +257,7 @@ std::vector<RunCtl> make_ctl(const muca_batch *b, const muca_batch_run_opts *o)
         std::memset(&c, 0, sizeof c);
         const uint32_t N = m.L * m.L;
         c.st.k = 0;
-        c.st.nup = o->starting_M;
+        c.st.nup = o->starting_sweeps ? o->starting_sweeps * N : o->starting_M;
         c.st.width = 10;
         c.st.total_run = (unsigned long long)c.st.nup * m.nchains;
         c.N = N;
@@ -267,6 +267,7 @@ std::vector<RunCtl> make_ctl(const muca_batch *b, const muca_batch_run_opts *o)
         c.flat_minmean = o->flat_minmean;
         c.max_iter = o->max_iter ? o->max_iter : 1000000u;
         c.sched = o->nup_schedule;
+        c.nup_max = o->nup_max;
         c.mom_thr = o->min_over_mean > 0 ? o->min_over_mean : 0.5;
         c.dkl_max = o->d_kl_max > 0 ? o->d_kl_max : 1e-4;
         c.recs = b->d_recs + i;
@@ -551,7 +552,10 @@ muca_status muca_batch_run(muca_batch *b, const muca_batch_run_opts *o, muca_bat
 {
     if (!b || !o) return bfail(b, MUCA_ERR_BAD_ARG, "NULL argument");
     if (o->rule > MUCA_UPDATE_RECURSION) return bfail(b, MUCA_ERR_BAD_ARG, "rule %u", o->rule);
-    if (o->starting_M == 0) return bfail(b, MUCA_ERR_BAD_ARG, "starting_M must be >= 1");
+    if (o->starting_M == 0 && o->starting_sweeps == 0)
+        return bfail(b, MUCA_ERR_BAD_ARG, "starting_M or starting_sweeps must be >= 1");
+    if (o->starting_sweeps > 4096) return bfail(b, MUCA_ERR_BAD_ARG, "starting_sweeps=%u (at most 4096)", o->starting_sweeps);
+    if (o->nup_schedule > 2) return bfail(b, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..2)", o->nup_schedule);
     const uint32_t K = o->graph_iters ? o->graph_iters : 16u;
     if (K > 4096) return bfail(b, MUCA_ERR_BAD_ARG, "graph_iters=%u (at most 4096)", K);
     BCUDA(b, cudaSetDevice(b->device));

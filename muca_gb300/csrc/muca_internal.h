@@ -116,7 +116,7 @@ struct RunCtl {
     IterState st;
     uint32_t N, nchains_total, rule, hold, flat_minmean, max_iter, sched, rec_cap;
     uint32_t rec_ring;  // 1: records go to recs[k % rec_cap] (streaming), else recs[k] for k < rec_cap
-    uint32_t pad_;
+    uint32_t nup_max;   // cap of NUPDATES (0: none for schedule 0, 2^30 for the doubling ones)
     double mom_thr, dkl_max;
     IterRecordDev *recs;
 };

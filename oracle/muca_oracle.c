@@ -591,9 +591,20 @@ unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int3
     for (unsigned i = 0; i <= N; i++) w[i] = (float)lnw[i];
     unsigned k;
     for (k = 0; k < o->max_iter; k++) {
-        if (width == N) {
-            NUPDATES = NUPDATES + 1;
-            NUPDATES = (unsigned)(NUPDATES * 1.01);
+        {
+            /* the schedule at the top of the loop (muca_delta_multigpu.cu:379-382),
+               with the doubling schedules and the cap as options */
+            uint64_t nx = NUPDATES;
+            unsigned cap = o->nup_max;
+            if ((o->sched == 2 && k > 0) || (o->sched == 1 && width == N)) {
+                nx = 2ull * NUPDATES;
+                if (cap == 0) cap = 1u << 30;
+            } else if (o->sched == 0 && width == N) {
+                const unsigned nu = NUPDATES + 1;
+                nx = (unsigned)(nu * 1.01);
+            }
+            if (cap != 0 && nx > cap) nx = cap > NUPDATES ? cap : NUPDATES;
+            NUPDATES = (unsigned)nx;
         }
         total_run += (uint64_t)NUPDATES * o->nchains;
         memset(h, 0, sizeof(uint64_t) * (N + 1));

@@ -42,7 +42,7 @@ class WeightOpts(C.Structure):
     _fields_ = [("L", C.c_uint), ("nchains", C.c_uint), ("jack", C.c_uint), ("gpu", C.c_uint),
                 ("starting_M", C.c_uint), ("recursive", C.c_int), ("hold_until_full", C.c_int),
                 ("flat_minmean", C.c_int), ("max_iter", C.c_uint), ("rounds", C.c_uint),
-                ("nthreads", C.c_int), ("width_start", C.c_uint)]
+                ("nthreads", C.c_int), ("width_start", C.c_uint), ("sched", C.c_uint), ("nup_max", C.c_uint)]
 
 
 def build(ref: bool = False, refgpu: bool = False) -> None:

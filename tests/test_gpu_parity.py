@@ -306,21 +306,27 @@ def test_weight_update_vs_oracle(muca, orc, rule, N):
             np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-9)
 
 
-@pytest.mark.parametrize("rule,hold,flat", [(0, 0, 0), (2, 0, 0), (0, 1, 0), (0, 0, 1), (1, 0, 0)])
-def test_weight_run_vs_oracle(muca, orc, rule, hold, flat):
+@pytest.mark.parametrize("rule,hold,flat,sched", [(0, 0, 0, 0), (2, 0, 0, 0), (0, 1, 0, 0), (0, 0, 1, 0),
+                                                   (1, 0, 0, 0), (0, 0, 1, 1), (2, 0, 1, 2), (0, 0, 1, 2)])
+def test_weight_run_vs_oracle(muca, orc, rule, hold, flat, sched):
     """Whole reference iteration loop (schedule, width, D_KL, update) on the
-    device against orc_weight_run, iteration by iteration."""
-    L, cpd, max_iter = 8, 256, 60
+    device against orc_weight_run, iteration by iteration; sched 1 and 2 are
+    the doubling schedules (once at full width / every iteration)."""
+    # doubling every iteration: few iterations, so the oracle stays quick
+    L, cpd, max_iter = 8, 256, (14 if sched == 2 else 60)
+    nup_max = 3000 if sched == 1 else 0
+    M = 64 if sched == 1 else 1  # reaches full width, then doubles up to the cap
     N = L * L
     with muca.Engine(L, nchains=cpd) as e:
-        res, recs = e.weight_run(starting_M=1, jack=0, rule=rule, hold_until_full=hold, flat_minmean=flat,
-                                 max_iter=max_iter, records=max_iter)
+        res, recs = e.weight_run(starting_M=M, jack=0, rule=rule, hold_until_full=hold, flat_minmean=flat,
+                                 max_iter=max_iter, nup_schedule=sched, nup_max=nup_max, records=max_iter)
         lat = e.get_lattice()
         w = e.get_weights()
     if rule == 1:
         pytest.skip("the CPU-flavour update has no oracle run loop; covered by test_weight_update_vs_oracle")
-    o = orc.WeightOpts(L=L, nchains=cpd, jack=0, gpu=0, starting_M=1, recursive=1 if rule == 2 else 0,
-                       hold_until_full=hold, flat_minmean=flat, max_iter=max_iter, rounds=7, nthreads=8)
+    o = orc.WeightOpts(L=L, nchains=cpd, jack=0, gpu=0, starting_M=M, recursive=1 if rule == 2 else 0,
+                       hold_until_full=hold, flat_minmean=flat, max_iter=max_iter, rounds=7, nthreads=8, sched=sched,
+                       nup_max=nup_max)
     olat = orc.init_lattice(L, cpd, orc.scheme_weight(0, 0)).reshape(-1).copy()
     oej, oed, _ = orc.energies(L, olat.reshape(cpd, N))
     lnw = np.zeros(N + 1)
