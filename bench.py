@@ -59,6 +59,7 @@ def parse():
     p.add_argument("--chains", type=int, default=CHAINS_DEFAULT)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ref-gpu", action="store_true")
+    p.add_argument("--no-extra", action="store_true", help="skip the flat-run, batch and production lines")
     return p.parse_args()
 
 
@@ -331,6 +332,12 @@ def ours_arm(args, ws, rank, local):
     eng.close()
     if rank == 0 and ws == 1 and not args.no_ref_gpu:
         out["ref_gpu_kernel"] = ref_gpu_kernel_rate(L, chains)
+    if rank == 0 and ws == 1 and not args.no_extra:
+        for key, fn in (("flat_run", flat_run_metric), ("batch", batch_metric), ("production", production_metric)):
+            try:
+                out[key] = fn(local)
+            except Exception as ex:  # an extra line never fails the bench
+                out[key] = {"error": str(ex)[:200]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         v, sample = cpu_oracle_rate(L, chains, nthreads)
@@ -342,6 +349,85 @@ def ours_arm(args, ws, rank, local):
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def flat_run_metric(local):
+    """Second metric of the L=72 configuration: weight iterations (and device
+    time) until the histogram is flat at min/mean >= 0.5.  The update is the
+    reference GPU program's trivial one (lnW -= ln H); the reference's
+    weight_recursion, run to the same criterion, does not flatten within
+    thousands of iterations from a zero weight."""
+    import muca_gb300 as m
+    L, nc = 72, 16384
+    N = L * L
+    with m.Engine(L, nchains=nc, device=local) as e:
+        res, _ = e.weight_run(starting_M=N, rule=m.UPDATE_TRIVIAL, nup_schedule=1, flat_minmean=1, max_iter=6000,
+                              nup_max=1 << 20, init_scheme=m.INIT_BASELINE, records=1)
+    return {"metric": "weight iterations to a flat histogram (min/mean >= 0.5) at L=72", "L": L, "chains": nc,
+            "iterations": res.iterations, "converged": bool(res.converged),
+            "width_reached_iteration": res.width_reached_iter, "device_s": res.total_kernel_s,
+            "wall_s": res.wall_s, "update": "trivial (lnW -= ln H for H > 1, then lnW -= lnW[0])",
+            "schedule": "NUPDATES = N, doubling once the width is N (cap 2^20)",
+            "init": "Philox4x32-10, key 2024, counter = chain id"}
+
+
+def batch_metric(local, iters=32):
+    """The batched engine on 256 uneven instances (L in {16..128}, T in
+    [0.4, 0.8], 256 chains each, seed = instance id): device throughput of
+    `iters` graph-captured iterations at NUPDATES = N per instance."""
+    import numpy as np
+    import muca_gb300 as m
+    Ls = [16, 24, 32, 48, 64, 72, 96, 128]
+    inst = []
+    for i in range(256):
+        r = np.random.default_rng(i)
+        inst.append((int(r.choice(Ls)), 256, 1.0 / float(r.uniform(0.4, 0.8)), i))
+    with m.Batch(inst, device=local) as b:
+        info = b.info()
+        res, sec = b.run(starting_sweeps=1, rule=m.UPDATE_TRIVIAL, nup_schedule=0, flat_minmean=1, max_iter=iters,
+                         graph_iters=iters)
+    att = sum(r.iterations * L * L * nc + r.total_run for r, (L, nc, _, _) in zip(res, inst))
+    return {"metric": "batched weight iterations, spin-flip attempts/ns", "value": att / (sec * 1e9),
+            "unit": "attempts/ns", "instances": len(inst), "iterations": iters, "attempts": att, "device_s": sec,
+            "shape": {"chains_per_block": info.shape.chains_per_block, "lattice_in_smem": info.shape.lattice_in_smem,
+                      "hist_in_smem": info.shape.hist_in_smem, "blocks_per_sm": info.shape.blocks_per_sm,
+                      "shapes_tried": info.n_tried},
+            "graph": "%d iterations (clear, persistent sweep, update) per CUDA graph" % iters}
+
+
+def production_metric(local):
+    """Production at L=128, 16384 chains (the L=128 configuration's shapes,
+    with the sweep counts scaled down): FP64 weights, 2D (E_Delta, M) u64
+    histogram of 134 M bins; then the reweighting of that histogram."""
+    import numpy as np
+    import torch
+    import muca_gb300 as m
+    L, nc = 128, 16384
+    N = L * L
+    stream = torch.cuda.Stream()
+    with m.Engine(L, nchains=nc, device=local, mode=m.MODE_PRODUCE, stream=stream.cuda_stream) as e:
+        e.init_chains(m.INIT_PRODUCE, 0)
+        e.set_weights(np.zeros(N + 1))
+        e.sweep(0, 100, 1000, N, 0)  # one thermalisation sweep
+        sweeps = 4
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        e.sweep(1, 100, 2000, 0, sweeps * N)
+        e1.record(stream)
+        e1.synchronize()
+        t_sweep = e0.elapsed_time(e1) * 1e-3
+        e.weight_shift(2.0, 1.96)
+        e.observables(2.0, 1.96)
+        t0 = time.perf_counter()
+        reps = 5
+        for _ in range(reps):
+            e.observables(2.0, 1.96)
+        t_obs = (time.perf_counter() - t0) / reps
+    bins = (N + 1) * (N + 2) // 2
+    return {"metric": "production sweep attempts/ns at L=128", "value": nc * sweeps * N / (t_sweep * 1e9),
+            "unit": "attempts/ns", "chains": nc, "sweeps": sweeps, "timing": "CUDA events around one launch",
+            "reweighting": {"bins": bins, "ms": 1e3 * t_obs, "GB_per_s": 8 * bins / t_obs / 1e9,
+                            "timing": "host clock, mean of %d calls (histogram read once per call)" % reps}}
 
 
 def ref_gpu_kernel_rate(L, chains):

@@ -121,7 +121,8 @@ typedef struct muca_run_opts {
     uint32_t init_scheme;   /* muca_init_scheme for the chains; MUCA_INIT_WEIGHT for parity */
     uint32_t reinit_chains; /* 1: initialise chains at the start (the reference does, :340-354) */
     uint32_t nup_schedule;  /* 0: reference ((NUP+1)*1.01 once width==N, :379-382); 1: doubling once
-                               width==N; 2: doubling every iteration from the first (cap 2^30) */
+                               width==N; 2: doubling every iteration from the first (cap 2^30);
+                               3: as 0, and doubling once every bin also holds >= 5 % of the mean */
     double min_over_mean;   /* threshold for flat_minmean (0 = 0.5) */
     double d_kl_max;        /* threshold of the D_KL test (0 = 1e-4) */
     uint32_t width_start;   /* initial running width (0 = 10, :314); the reference keeps the
@@ -297,7 +298,8 @@ typedef struct muca_batch_run_opts {
     uint32_t starting_M;    /* initial NUPDATES of every instance */
     uint32_t rule;          /* muca_update_rule */
     uint32_t nup_schedule;  /* 0: (NUP+1)*1.01 once width == N (:379-382); 1: doubling once width == N;
-                               2: doubling every iteration (cap 2^30) */
+                               2: doubling every iteration (cap 2^30); 3: as 0, doubling once every
+                               bin also holds >= 5 % of the mean count */
     uint32_t flat_minmean;  /* 0: stop at width == N && D_KL < d_kl_max; 1: at min/mean >= min_over_mean */
     uint32_t max_iter;      /* per instance (0 = 1000000) */
     uint32_t graph_iters;   /* iterations per captured graph (0 = 16) */
@@ -333,6 +335,35 @@ muca_status muca_batch_get_histogram(muca_batch *b, uint32_t i, uint64_t *hist, 
  * device time.  MUCA_ERR_NOT_CONVERGED if some instance hit max_iter. */
 muca_status muca_batch_run(muca_batch *b, const muca_batch_run_opts *opts, muca_batch_result *res,
                            double *seconds);
+
+/* ---- Learned warm start (no counterpart in the reference) ----
+ * A multilayer perceptron (L/128, T, Delta, E_Delta/N) -> (lnW - mean lnW)/N,
+ * three hidden layers of 128 SiLU units, FP32, trained with Adam on the
+ * device by this library's own kernels.  Its prediction replaces the zero or
+ * extrapolated initial weight of the reference's `continuing` path
+ * (muca_delta_multigpu.cu:223-235); the weight iteration then runs to its
+ * usual stop criterion.  Parameters: one flat FP32 array of
+ * muca_mlp_param_count() values, per layer the [out][in] matrix then the bias. */
+typedef struct muca_mlp muca_mlp;
+size_t muca_mlp_param_count(void);
+/* seed: initial parameters uniform in +-1/sqrt(fan_in) from splitmix64(seed) */
+muca_status muca_mlp_create(int32_t device, uint64_t seed, void *stream, muca_mlp **out);
+muca_status muca_mlp_destroy(muca_mlp *m);
+const char *muca_mlp_last_error(const muca_mlp *m); /* NULL: errors of muca_mlp_create */
+muca_status muca_mlp_get_params(muca_mlp *m, float *params, size_t n);
+/* also resets the Adam moments and step count */
+muca_status muca_mlp_set_params(muca_mlp *m, const float *params, size_t n);
+/* training set: x [n][4] = (L/128, T, Delta, E_Delta/N), t [n] = (lnW - mean)/N */
+muca_status muca_mlp_set_data(muca_mlp *m, const float *x, const float *t, uint32_t n);
+/* `steps` Adam steps (lr, beta 0.9/0.999, eps 1e-8) on minibatches of `batch`
+ * points drawn with Philox(seed, step); losses (steps values, may be NULL)
+ * gets each step's mean squared error. */
+muca_status muca_mlp_train(muca_mlp *m, uint32_t steps, uint32_t batch, float lr, uint32_t seed, float *losses);
+/* gradient of the mean squared error over (x, t) (n points) without a step */
+muca_status muca_mlp_grad(muca_mlp *m, const float *x, const float *t, uint32_t n, float *grad, float *loss);
+muca_status muca_mlp_predict(muca_mlp *m, const float *x, uint32_t n, float *y);
+/* lnW[0..N] for (L, T, Delta): N * (y(i/N) - y(0)), ready for muca_set_weights */
+muca_status muca_mlp_log_weights(muca_mlp *m, uint32_t L, double T, double delta, double *lnw, size_t n);
 
 #ifdef __cplusplus
 }

@@ -38,6 +38,9 @@ EXPORTS = [
     "muca_batch_create", "muca_batch_destroy", "muca_batch_last_error", "muca_batch_get_info",
     "muca_batch_init_chains", "muca_batch_set_weights", "muca_batch_get_weights", "muca_batch_get_histogram",
     "muca_batch_run",
+    "muca_mlp_param_count", "muca_mlp_create", "muca_mlp_destroy", "muca_mlp_last_error", "muca_mlp_get_params",
+    "muca_mlp_set_params", "muca_mlp_set_data", "muca_mlp_train", "muca_mlp_grad", "muca_mlp_predict",
+    "muca_mlp_log_weights",
 ]
 
 
@@ -187,6 +190,19 @@ def lib():
     L.muca_batch_get_weights.argtypes = [vp, C.c_uint32, f64, C.c_size_t]
     L.muca_batch_get_histogram.argtypes = [vp, C.c_uint32, u64, C.c_size_t]
     L.muca_batch_run.argtypes = [vp, C.POINTER(BatchRunOpts), C.POINTER(BatchResult), C.POINTER(C.c_double)]
+    f32 = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    L.muca_mlp_param_count.restype = C.c_size_t
+    L.muca_mlp_create.argtypes = [C.c_int32, C.c_uint64, vp, C.POINTER(vp)]
+    L.muca_mlp_destroy.argtypes = [vp]
+    L.muca_mlp_last_error.argtypes = [vp]
+    L.muca_mlp_last_error.restype = C.c_char_p
+    L.muca_mlp_get_params.argtypes = [vp, f32, C.c_size_t]
+    L.muca_mlp_set_params.argtypes = [vp, f32, C.c_size_t]
+    L.muca_mlp_set_data.argtypes = [vp, f32, f32, C.c_uint32]
+    L.muca_mlp_train.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, vp]
+    L.muca_mlp_grad.argtypes = [vp, f32, f32, C.c_uint32, f32, C.POINTER(C.c_float)]
+    L.muca_mlp_predict.argtypes = [vp, f32, C.c_uint32, f32]
+    L.muca_mlp_log_weights.argtypes = [vp, C.c_uint32, C.c_double, C.c_double, f64, C.c_size_t]
     _LIB = L
     return L
 
@@ -439,3 +455,92 @@ class Batch:
         self._ck(self._lib.muca_batch_run(self._h, C.byref(o), res, C.byref(sec)),
                  allow=() if raise_on_not_converged else (4,))
         return list(res), sec.value
+
+
+
+class MLP:
+    """The warm-start network (muca_mlp_*): (L/128, T, Delta, E_Delta/N) ->
+    (lnW - mean lnW)/N, 3 x 128 SiLU, FP32, trained on the device."""
+
+    def __init__(self, device=0, seed=0, stream=None):
+        self._lib = lib()
+        h = C.c_void_p()
+        st = self._lib.muca_mlp_create(device, seed, C.c_void_p(stream) if stream else None, C.byref(h))
+        if st:
+            raise MucaError(st, self._lib.muca_mlp_last_error(None).decode())
+        self._h = h
+        self.n_params = int(self._lib.muca_mlp_param_count())
+
+    def _ck(self, st):
+        if st:
+            raise MucaError(st, self._lib.muca_mlp_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.muca_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def params(self):
+        p = np.zeros(self.n_params, np.float32)
+        self._ck(self._lib.muca_mlp_get_params(self._h, p, p.size))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        self._ck(self._lib.muca_mlp_set_params(self._h, p, p.size))
+
+    def set_data(self, x, t):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 4)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1)
+        assert x.shape[0] == t.size
+        self._ck(self._lib.muca_mlp_set_data(self._h, x, t, t.size))
+
+    def train(self, steps, batch=4096, lr=1e-3, seed=0):
+        losses = np.zeros(steps, np.float32)
+        self._ck(self._lib.muca_mlp_train(self._h, steps, batch, lr, seed, losses.ctypes.data))
+        return losses
+
+    def grad(self, x, t):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 4)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1)
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_float()
+        self._ck(self._lib.muca_mlp_grad(self._h, x, t, t.size, g, C.byref(loss)))
+        return loss.value, g
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 4)
+        y = np.zeros(x.shape[0], np.float32)
+        self._ck(self._lib.muca_mlp_predict(self._h, x, x.shape[0], y))
+        return y
+
+    def log_weights(self, L, T, delta):
+        w = np.zeros(L * L + 1)
+        self._ck(self._lib.muca_mlp_log_weights(self._h, L, T, delta, w, w.size))
+        return w
+
+
+def mlp_features(L, T, delta, lnw):
+    """Training pairs of one converged weight: x = (L/128, T, Delta, i/N),
+    t = (lnW_i - mean lnW)/N for i = 0..N."""
+    lnw = np.asarray(lnw, np.float64)
+    N = lnw.size - 1
+    x = np.zeros((N + 1, 4), np.float32)
+    x[:, 0] = L / 128.0
+    x[:, 1] = T
+    x[:, 2] = delta
+    x[:, 3] = np.arange(N + 1) / N
+    t = ((lnw - lnw.mean()) / N).astype(np.float32)
+    return x, t

@@ -49,15 +49,19 @@ struct AddD { __device__ double operator()(double a, double b) const { return a 
 // ctl != nullptr: one iteration of a device-driven run (see RunCtl).
 // NUPDATES of the next iteration.  sched 0: the reference's (NUP+1)*1.01
 // once the width is full (muca_delta_multigpu.cu:379-382); 1: doubling once
-// the width is full; 2: doubling every iteration.  The result is capped at
-// `cap` (0: no cap for sched 0, 2^30 for doubling) but never falls below nup.
-__host__ __device__ __forceinline__ uint32_t next_nupdates(uint32_t nup, bool full, uint32_t sched, uint32_t cap)
+// the width is full; 2: doubling every iteration; 3: the reference's growth
+// once the width is full and doubling once, in addition, every bin of this
+// iteration's histogram holds at least 5 % of the mean count (`covered`).
+// The result is capped at `cap` (0: no cap for sched 0, 2^30 for doubling)
+// but never falls below nup.
+__host__ __device__ __forceinline__ uint32_t next_nupdates(uint32_t nup, bool full, bool covered, uint32_t sched,
+                                                           uint32_t cap)
 {
     unsigned long long nx = nup;
-    if (sched == 2 || (sched == 1 && full)) {
+    if (sched == 2 || (sched == 1 && full) || (sched == 3 && full && covered)) {
         nx = 2ull * nup;
         if (cap == 0) cap = 1u << 30;
-    } else if (sched == 0 && full) {
+    } else if ((sched == 0 || sched == 3) && full) {
         const unsigned nu = nup + 1u;
         nx = (unsigned)(nu * 1.01);
     }
@@ -147,7 +151,7 @@ __device__ __forceinline__ void weight_update_body(const unsigned long long *__r
                 if (st.k >= ctl->max_iter) {
                     st.stop = 1;
                 } else {
-                    st.nup = next_nupdates(st.nup, st.width == N, ctl->sched, ctl->nup_max);
+                    st.nup = next_nupdates(st.nup, st.width == N, mom >= 0.05, ctl->sched, ctl->nup_max);
                     st.total_run += (unsigned long long)st.nup * ctl->nchains_total;
                 }
             }

@@ -528,7 +528,7 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "weight run needs a weight-mode context");
     if (o->rule > MUCA_UPDATE_RECURSION) return fail(c, MUCA_ERR_BAD_ARG, "rule %u", o->rule);
     if (o->starting_M == 0) return fail(c, MUCA_ERR_BAD_ARG, "starting_M must be >= 1");
-    if (o->nup_schedule > 2) return fail(c, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..2)", o->nup_schedule);
+    if (o->nup_schedule > 3) return fail(c, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..3)", o->nup_schedule);
     CUDA_TRY(c, cudaSetDevice(c->device));
     const auto t0 = std::chrono::steady_clock::now();
     if (o->reinit_chains) {
@@ -551,8 +551,9 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     // starts at full width (a later jack) grows NUPDATES before its first sweep;
     // the device applies it between iterations from then on
     if (h.st.width == c->N && o->nup_schedule != 2) {
-        unsigned long long nx = o->nup_schedule ? 2ull * h.st.nup : (unsigned)((h.st.nup + 1u) * 1.01);
-        const uint32_t cap = o->nup_max ? o->nup_max : (o->nup_schedule ? (1u << 30) : 0u);
+        // (schedule 3 knows no histogram yet: it grows like the reference's)
+        unsigned long long nx = o->nup_schedule == 1 ? 2ull * h.st.nup : (unsigned)((h.st.nup + 1u) * 1.01);
+        const uint32_t cap = o->nup_max ? o->nup_max : (o->nup_schedule == 1 ? (1u << 30) : 0u);
         if (cap != 0 && nx > cap) nx = cap > h.st.nup ? cap : h.st.nup;
         h.st.nup = (uint32_t)nx;
     }

@@ -180,6 +180,20 @@ size_t observables_static_partials();
 cudaError_t launch_observables_static(int device, const unsigned long long *hist2d, const double *lnw, uint32_t N,
                                       double beta, double delta, double *out, cudaStream_t s);
 
+// Warm-start MLP (k_mlp.cu): 4 -> 128 -> 128 -> 128 -> 1, SiLU, FP32.
+size_t mlp_param_count();
+cudaError_t mlp_prepare();  // shared-memory limits (call before any capture)
+// scratch floats of a minibatch of B points: Xb [B][4], Tb [B], Y [B], Z, dZ, partials
+size_t mlp_scratch_floats(uint32_t B);
+// Y[0..B) = net(Xb) (Z: pre-activations [3][B][128] or NULL)
+cudaError_t launch_mlp_forward(const float *P, const float *Xb, uint32_t B, float *Z, float *Y, cudaStream_t s);
+// Gradient of the mean squared error on a minibatch (drawn from (X, T, n)
+// when gather, else already in scratch) into G; with m and v also one Adam
+// step; the loss goes to losses[*step - *base] (or losses[0] without step).
+cudaError_t launch_mlp_step(float *P, float *G, float *m, float *v, const float *X, const float *T, uint32_t n,
+                            uint32_t B, uint32_t *step, const uint32_t *base, uint32_t seed, bool gather, float lr,
+                            float *scratch, float *losses, uint32_t losses_cap, cudaStream_t s);
+
 // Philox throughput microbenchmark (k_bench.cu): grid blocks of 256 threads,
 // each generating blocks_per_thread Philox4x32-R blocks.
 cudaError_t launch_philox_peak(int rounds, uint32_t grid, uint32_t blocks_per_thread, uint32_t *out, cudaStream_t s);

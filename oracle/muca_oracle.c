@@ -587,19 +587,23 @@ unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int3
     unsigned width = o->width_start ? o->width_start : 10, NUPDATES = o->starting_M;
     int reach = 0;
     uint64_t total_run = 0;
+    double prev_mm = 0.0;
     *converged = 0;
     for (unsigned i = 0; i <= N; i++) w[i] = (float)lnw[i];
     unsigned k;
     for (k = 0; k < o->max_iter; k++) {
         {
             /* the schedule at the top of the loop (muca_delta_multigpu.cu:379-382),
-               with the doubling schedules and the cap as options */
+               with the doubling schedules and the cap as options; schedule 3
+               doubles once the previous iteration's histogram also had every
+               bin at >= 5 % of the mean */
             uint64_t nx = NUPDATES;
             unsigned cap = o->nup_max;
-            if ((o->sched == 2 && k > 0) || (o->sched == 1 && width == N)) {
+            if ((o->sched == 2 && k > 0) || (o->sched == 1 && width == N) ||
+                (o->sched == 3 && width == N && k > 0 && prev_mm >= 0.05)) {
                 nx = 2ull * NUPDATES;
                 if (cap == 0) cap = 1u << 30;
-            } else if (o->sched == 0 && width == N) {
+            } else if ((o->sched == 0 || o->sched == 3) && width == N) {
                 const unsigned nu = NUPDATES + 1;
                 nx = (unsigned)(nu * 1.01);
             }
@@ -618,6 +622,7 @@ unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int3
         double mm;
         int a, b;
         orc_flatness(h, N, &mm, &a, &b);
+        prev_mm = mm;
         if (k < rec_cap) {
             rec[k * 5 + 0] = width_temp;
             rec[k * 5 + 1] = dkl;

@@ -125,7 +125,8 @@ typedef struct orc_weight_opts {
     int nthreads;
     unsigned width_start; /* initial running width; 0 = 10 (the reference keeps the previous jack's) */
     unsigned sched;       /* NUPDATES schedule: 0 reference ((NUP+1)*1.01 once width==N), 1 doubling
-                             once width==N, 2 doubling every iteration from the first */
+                             once width==N, 2 doubling every iteration from the first, 3 as 0 and
+                             doubling once the last histogram had every bin >= 5 % of the mean */
     unsigned nup_max;     /* cap of NUPDATES: 0 = none for schedule 0, 2^30 for doubling; never decreases */
 } orc_weight_opts;
 unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int32_t *edel,
