@@ -60,6 +60,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ref-gpu", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the flat-run, batch and production lines")
+    p.add_argument("--kernel", type=int, default=0, help="sweep kernel: 0 auto, 1 generic, 2 windowed, 3 specialised")
     return p.parse_args()
 
 
@@ -223,7 +224,7 @@ def ours_arm(args, ws, rank, local):
     N = L * L
     attempts_per_step = chains * 2 * N
     stream = torch.cuda.Stream()
-    eng = m.Engine(L, nchains=chains, device=local, stream=stream.cuda_stream, dev_offset=rank)
+    eng = m.Engine(L, nchains=chains, device=local, stream=stream.cuda_stream, dev_offset=rank, kernel=args.kernel)
     eng.init_chains(m.INIT_WEIGHT, 0)
     eng.set_weights(np.zeros(N + 1))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
