@@ -60,8 +60,17 @@ typedef enum muca_init_scheme {
     MUCA_INIT_PRODUCE = 1,  /* produce2_multigpu.cu:126-138: key {10W, 0xdecafbad},
                                ctr {1000*dev, 100, 0, 0xBADCAFE3}, ++ctr[2] per 4 sites */
     MUCA_INIT_BASELINE = 2, /* extension: Philox4x32-10, key {2024, jack}, ctr {chain, group, 0, 0} */
-    MUCA_INIT_ORDERED = 3   /* extension for rand_config=0: every spin +1 */
+    MUCA_INIT_ORDERED = 3,  /* extension for rand_config=0: every spin +1 */
+    MUCA_INIT_MUCA_MAG = 4  /* muca_mag.cpp:63-73 (the CPU weight program): key {10W + 10000*jack,
+                               0xdecafbad}, ctr {0, 100, 0xBADCAB1E, 0xBADC0DED}, ++ctr[0] per 4 sites */
 } muca_init_scheme;
+
+typedef enum muca_algorithm {
+    MUCA_ALGO_SWEEP = 0,      /* the GPU programs' kernels: sites in sweep order, two Philox streams */
+    MUCA_ALGO_RANDOM_SITE = 1 /* the CPU weight program's mcs (muca_mag.cpp:312-393) and its GPU port
+                                 mcs2 (muca_delta_multigpu.cu:637-734): random site, three Philox
+                                 streams, FP64 weights; weight mode only */
+} muca_algorithm;
 
 typedef enum muca_update_rule {
     MUCA_UPDATE_TRIVIAL = 0,     /* muca_delta_multigpu.cu:466-476: lnW -= ln H for H>1; lnW -= lnW[0] */
@@ -83,6 +92,9 @@ typedef struct muca_params {
                             counters follow the device index) */
     uint32_t kernel;     /* sweep kernel: 0 auto, 1 generic (reference step by step),
                             2 windowed, 3 warp-specialised (2 and 3 need L % 8 == 0) */
+    uint32_t algorithm;  /* muca_algorithm */
+    uint32_t host_logf;  /* random-site algorithm: 1 = the acceptance log is the host libm's logf
+                            (what the CPU program computes; bit-exact with it), 0 = CUDA's logf (mcs2) */
 } muca_params;
 
 typedef struct muca_info {
@@ -112,7 +124,8 @@ typedef struct muca_hist_stats {
 typedef struct muca_run_opts {
     uint32_t jack;          /* jack index mm (init key 10W + 2*mm) */
     uint32_t starting_M;    /* initial NUPDATES (argv[5]) */
-    uint32_t therm;         /* thermalisation attempts per chain per iteration; 0 = N (therm_coeff*N) */
+    uint32_t therm;         /* thermalisation attempts per chain per iteration; 0 = N (therm_coeff*N),
+                               or 0 for the random-site algorithm (muca_mag.cpp:140) */
     uint32_t rule;          /* muca_update_rule */
     uint32_t hold_until_full; /* 1: no update before width==N (muca_mag.cpp:170-177 intent);
                                  0: update every iteration (what the GPU program does, :466) */
@@ -122,7 +135,8 @@ typedef struct muca_run_opts {
     uint32_t reinit_chains; /* 1: initialise chains at the start (the reference does, :340-354) */
     uint32_t nup_schedule;  /* 0: reference ((NUP+1)*1.01 once width==N, :379-382); 1: doubling once
                                width==N; 2: doubling every iteration from the first (cap 2^30);
-                               3: as 0, and doubling once every bin also holds >= 5 % of the mean */
+                               3: as 0, and doubling once every bin also holds >= 5 % of the mean;
+                               4: NUP*1.05 every iteration, the first included (muca_mag.cpp:131) */
     double min_over_mean;   /* threshold for flat_minmean (0 = 0.5) */
     double d_kl_max;        /* threshold of the D_KL test (0 = 1e-4) */
     uint32_t width_start;   /* initial running width (0 = 10, :314); the reference keeps the
@@ -179,7 +193,10 @@ muca_status muca_get_weights(muca_ctx *ctx, double *lnw, size_t n);
  * mcs (muca_delta_multigpu.cu:393 / produce2_multigpu.cu:301,311).  The
  * histogram is cleared first (the reference clears it inside the kernel,
  * racily, :746-749).  seed of emulated device d = seed_base + seed_dev_mul*d
- * (the reference passes SEED+1000*l, SEED+1000*GPU+l, SEED+2000*GPU). */
+ * (the reference passes SEED+1000*l, SEED+1000*GPU+l, SEED+2000*GPU).
+ * Random-site algorithm: one call of the CPU program's mcs (muca_mag.cpp:312)
+ * for every chain, with WORKER = chain, iter = `iter` and its `seed`
+ * argument (the jack index) = seed_base; seed_dev_mul is not used. */
 muca_status muca_sweep(muca_ctx *ctx, uint32_t iter, uint32_t seed_base, uint32_t seed_dev_mul,
                        uint64_t therm, uint64_t nup);
 /* Same, but accumulate into the histogram instead of clearing it. */

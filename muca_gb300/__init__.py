@@ -21,7 +21,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libmuca.so")
 
 MODE_WEIGHT, MODE_PRODUCE = 0, 1
-INIT_WEIGHT, INIT_PRODUCE, INIT_BASELINE, INIT_ORDERED = 0, 1, 2, 3
+INIT_WEIGHT, INIT_PRODUCE, INIT_BASELINE, INIT_ORDERED, INIT_MUCA_MAG = 0, 1, 2, 3, 4
+ALGO_SWEEP, ALGO_RANDOM_SITE = 0, 1
 UPDATE_TRIVIAL, UPDATE_TRIVIAL_CPU, UPDATE_RECURSION = 0, 1, 2
 KERNEL_AUTO, KERNEL_GENERIC, KERNEL_WINDOWED, KERNEL_SPECIALIZED = 0, 1, 2, 3
 STATUS = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "TIMEOUT", 4: "NOT_CONVERGED", 5: "IO", 6: "STATE"}
@@ -53,7 +54,7 @@ class MucaError(RuntimeError):
 class Params(C.Structure):
     _fields_ = [("L", C.c_uint32), ("nchains", C.c_uint32), ("ndev", C.c_uint32), ("device", C.c_int32),
                 ("rounds", C.c_uint32), ("mode", C.c_uint32), ("stream", C.c_void_p), ("dev_offset", C.c_uint32),
-                ("kernel", C.c_uint32)]
+                ("kernel", C.c_uint32), ("algorithm", C.c_uint32), ("host_logf", C.c_uint32)]
 
 
 class Info(C.Structure):
@@ -237,10 +238,11 @@ class Engine:
     """One simulation context (all chains of one lattice size) on one GPU."""
 
     def __init__(self, L, nchains=0, ndev=1, mode=MODE_WEIGHT, rounds=7, device=0, stream=None, dev_offset=0,
-                 kernel=KERNEL_AUTO):
+                 kernel=KERNEL_AUTO, algorithm=ALGO_SWEEP, host_logf=0):
         self._lib = lib()
         p = Params(L=L, nchains=nchains, ndev=ndev, device=device, rounds=rounds, mode=mode,
-                   stream=C.c_void_p(stream) if stream else None, dev_offset=dev_offset, kernel=kernel)
+                   stream=C.c_void_p(stream) if stream else None, dev_offset=dev_offset, kernel=kernel,
+                   algorithm=algorithm, host_logf=host_logf)
         h = C.c_void_p()
         st = self._lib.muca_create(C.byref(p), C.byref(h))
         if st:

@@ -23,7 +23,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE,
                      "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-CU_SOURCES = ["k_sweep.cu", "k_lattice.cu", "k_weights.cu", "k_observables.cu", "k_bench.cu", "k_batch.cu",
+CU_SOURCES = ["k_sweep.cu", "k_sweep_random.cu", "k_lattice.cu", "k_weights.cu", "k_observables.cu", "k_bench.cu", "k_batch.cu",
               "k_mlp.cu", "muca_api.cu", "muca_batch.cu", "muca_mlp.cu"]
 CLI_SOURCES = {"multigpu_weight": "multigpu_weight.cpp", "produce_gpu": "produce_gpu.cpp"}
 

@@ -8,8 +8,8 @@
 // (:520-535).  The triangle's row i (E_Delta = i) holds the i+1 bins
 // m = -i, -i+2, ..., i at (i^2 + 2i + m)/2 = i(i+1)/2 + (m+i)/2.
 //
-// The sums stream the u64 histogram once (HBM bound at 8 B per bin); empty
-// bins cost no FP64 work.  Each term is formed as the reference forms it:
+// The sums stream the u64 histogram once (HBM bound at 8 B per bin), one
+// warp per row; empty bins cost no FP64 work.  Each term is formed as the reference forms it:
 // (double)(|m| H) * boltz_i, (double)(m^2 H) * boltz_i; partial sums are
 // combined per warp, per block and then in a fixed-order second pass, so the
 // result is deterministic and agrees with the long-double host sum to ~1e-15.
@@ -47,46 +47,45 @@ __global__ void k_weight_shift(double *lnw, uint32_t N, double beta, double delt
     for (uint32_t i = threadIdx.x; i <= N; i += blockDim.x) lnw[i] = __dadd_rn(lnw[i], m);
 }
 
-// Row i of the first bin b: largest i with i(i+1)/2 <= b.
-__device__ __forceinline__ uint32_t row_of(unsigned long long b)
-{
-    uint32_t i = (uint32_t)((sqrt(8.0 * (double)b + 1.0) - 1.0) * 0.5);
-    while ((unsigned long long)i * (i + 1) / 2 > b) --i;
-    while ((unsigned long long)(i + 1) * (i + 2) / 2 <= b) ++i;
-    return i;
-}
+// One warp per row of the triangle at a time (row i = E_Delta holds the i+1
+// bins m = -i, -i+2, ..., i from b = i(i+1)/2): the lanes stream the row's
+// u64 counts with coalesced loads, kObsUnroll independent loads per lane in
+// flight, and boltz_i is formed once per row.  Warp w takes rows w, w + W,
+// w + 2W, ... (W warps in the grid), which spreads the long rows evenly.
+constexpr int kObsUnroll = 8;
 
 __global__ void __launch_bounds__(kObsThreads) k_observables(const unsigned long long *__restrict__ hist,
                                                              const double *__restrict__ lnw, uint32_t N,
                                                              double beta, double delta,
                                                              double *__restrict__ partials)
 {
-    const unsigned long long nb = (unsigned long long)(N + 1) * (N + 2) / 2;
     const double nbd = __dmul_rn(-beta, delta);
     double s0 = 0, s1 = 0, s2 = 0, s4 = 0;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    unsigned long long b = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    if (b < nb) {
-        uint32_t i = row_of(b);
-        unsigned long long row0 = (unsigned long long)i * (i + 1) / 2;
-        double bz = exp(__dsub_rn(__dmul_rn(nbd, (double)i), lnw[i]));
-        for (; b < nb; b += stride) {
-            while (b >= row0 + i + 1) {
-                row0 += i + 1;
-                ++i;
-                bz = -1.0;  // recomputed below when a nonzero bin needs it
+    const uint32_t ln = threadIdx.x & 31u;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i <= N; i += nwarps) {
+        const unsigned long long *row = hist + (unsigned long long)i * (i + 1) / 2;
+        const double bz = exp(__dsub_rn(__dmul_rn(nbd, (double)i), lnw[i]));
+        for (uint32_t j0 = 0; j0 <= i; j0 += 32u * kObsUnroll) {
+            unsigned long long h[kObsUnroll];
+#pragma unroll
+            for (int k = 0; k < kObsUnroll; ++k) {
+                const uint32_t j = j0 + ln + 32u * k;
+                h[k] = j <= i ? __ldcs(row + j) : 0ull;
             }
-            const unsigned long long H = __ldcs(hist + b);
-            if (H == 0) continue;
-            if (bz < 0.0) bz = exp(__dsub_rn(__dmul_rn(nbd, (double)i), lnw[i]));
-            const int m = 2 * (int)(b - row0) - (int)i;
-            const unsigned long long am = (unsigned long long)(m < 0 ? -m : m);
-            const double t0 = __dmul_rn((double)H, bz);
-            const double t2 = __dmul_rn((double)(am * am * H), bz);
-            s0 = __dadd_rn(s0, t0);
-            s1 = __dadd_rn(s1, __dmul_rn((double)(am * H), bz));
-            s2 = __dadd_rn(s2, t2);
-            s4 = __dadd_rn(s4, __dmul_rn(t2, (double)(am * am)));
+#pragma unroll
+            for (int k = 0; k < kObsUnroll; ++k) {
+                const unsigned long long H = h[k];
+                if (H == 0) continue;
+                const int m = 2 * (int)(j0 + ln + 32u * k) - (int)i;
+                const unsigned long long am = (unsigned long long)(m < 0 ? -m : m);
+                const double t0 = __dmul_rn((double)H, bz);
+                const double t2 = __dmul_rn((double)(am * am * H), bz);
+                s0 = __dadd_rn(s0, t0);
+                s1 = __dadd_rn(s1, __dmul_rn((double)(am * H), bz));
+                s2 = __dadd_rn(s2, t2);
+                s4 = __dadd_rn(s4, __dmul_rn(t2, (double)(am * am)));
+            }
         }
     }
     __shared__ double sh[4][kObsThreads / 32];

@@ -51,9 +51,10 @@ struct AddD { __device__ double operator()(double a, double b) const { return a 
 // once the width is full (muca_delta_multigpu.cu:379-382); 1: doubling once
 // the width is full; 2: doubling every iteration; 3: the reference's growth
 // once the width is full and doubling once, in addition, every bin of this
-// iteration's histogram holds at least 5 % of the mean count (`covered`).
-// The result is capped at `cap` (0: no cap for sched 0, 2^30 for doubling)
-// but never falls below nup.
+// iteration's histogram holds at least 5 % of the mean count (`covered`);
+// 4: NUP * 1.05 every iteration, truncated (the CPU program,
+// muca_mag.cpp:131).  The result is capped at `cap` (0: no cap for sched 0,
+// 2^30 otherwise) but never falls below nup.
 __host__ __device__ __forceinline__ uint32_t next_nupdates(uint32_t nup, bool full, bool covered, uint32_t sched,
                                                            uint32_t cap)
 {
@@ -64,6 +65,9 @@ __host__ __device__ __forceinline__ uint32_t next_nupdates(uint32_t nup, bool fu
     } else if ((sched == 0 || sched == 3) && full) {
         const unsigned nu = nup + 1u;
         nx = (unsigned)(nu * 1.01);
+    } else if (sched == 4) {
+        nx = (unsigned long long)((double)nup * 1.05);
+        if (cap == 0) cap = 1u << 30;
     }
     if (cap != 0 && nx > cap) nx = cap > nup ? cap : nup;
     return (uint32_t)nx;

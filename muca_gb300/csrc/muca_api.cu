@@ -46,6 +46,8 @@ struct muca_ctx {
     unsigned int *d_err = nullptr, *h_err = nullptr;
     uint64_t device_bytes = 0;
     double log_eps = 0;
+    uint32_t algo = 0;
+    float *d_logf_tab = nullptr;  // random-site algorithm with host_logf: the host libm's logf
     std::string err;
 };
 
@@ -82,7 +84,7 @@ void free_all(muca_ctx *c)
 {
     void *dp[] = {c->d_lat, c->d_ej, c->d_edel, c->d_mag, c->d_lnw, c->d_lnw_obs, c->d_pacc, c->d_w32, c->d_hist,
                   c->d_index, c->d_naver, c->d_stats, c->d_ctl, c->d_recs, c->d_obs_part, c->d_obs_out,
-                  c->d_jk, c->d_tmp, c->d_bad, c->d_err};
+                  c->d_jk, c->d_tmp, c->d_bad, c->d_err, c->d_logf_tab};
     for (void *p : dp)
         if (p) cudaFree(p);
     void *hp[] = {c->h_stats, c->h_ctl, c->h_obs_out, c->h_bad, c->h_err};
@@ -171,6 +173,30 @@ SweepArgs sweep_args(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint32_t se
     return a;
 }
 
+// Arguments of the random-site sweep (muca_mag.cpp:312-318): WORKER = chain
+// (offset by the first emulated device's chains), `seed` = the jack index.
+RandomArgs random_args(muca_ctx *c, uint32_t iter, uint32_t seed, uint64_t therm, uint64_t nup)
+{
+    RandomArgs a{};
+    a.lat = c->d_lat;
+    a.ej = c->d_ej;
+    a.edel = c->d_edel;
+    a.w = c->d_lnw;
+    a.hist = c->d_hist;
+    a.L = c->L;
+    a.N = c->N;
+    a.WPR = c->WPR;
+    a.nchains = c->nchains;
+    a.worker0 = 0;  // WORKER = chain: the CPU program's ranks; dev_offset does not apply
+    a.seed = seed;
+    a.iter = iter;
+    a.therm = therm;
+    a.nup = nup;
+    a.logf_tab = c->d_logf_tab;
+    a.dyn = nullptr;
+    return a;
+}
+
 }  // namespace
 
 extern "C" {
@@ -237,6 +263,15 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
         fail(c, MUCA_ERR_BAD_ARG, "kernel %u needs L %% 8 == 0", p->kernel);
         return bail(MUCA_ERR_BAD_ARG);
     }
+    if (p->algorithm > MUCA_ALGO_RANDOM_SITE) {
+        fail(c, MUCA_ERR_BAD_ARG, "algorithm=%u (0..1)", p->algorithm);
+        return bail(MUCA_ERR_BAD_ARG);
+    }
+    if (p->algorithm == MUCA_ALGO_RANDOM_SITE && (p->mode != MUCA_MODE_WEIGHT || p->L < 3 || c->ndev != 1)) {
+        fail(c, MUCA_ERR_BAD_ARG, "the random-site algorithm needs weight mode, L >= 3 and one device");
+        return bail(MUCA_ERR_BAD_ARG);
+    }
+    c->algo = p->algorithm;
     const int want_kernel = p->kernel == 0 ? -1 : (int)p->kernel - 1;
     c->plan = plan_sweep((int)c->mode, (int)rounds, c->L, c->nchains, c->smem_optin, c->sms, want_kernel);
     if (c->plan.smem > c->smem_optin) {
@@ -303,6 +338,21 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
         // anything else keeps every decision on the exact logf
         c->log_eps = (m >= 0.0f && m < 1e-2f) ? 2.0 * (double)m + 1e-30 : 1e30;
     }
+    if (c->algo == MUCA_ALGO_RANDOM_SITE) {
+        if (random_sweep_smem(c->L, c->plan.cpb, false) > c->smem_optin) {
+            fail(c, MUCA_ERR_BAD_ARG, "L=%u: FP64 weights and histogram exceed shared memory", c->L);
+            return bail(MUCA_ERR_BAD_ARG);
+        }
+        if (p->host_logf) {
+            // the CPU program's acceptance log, logf(u) of this host's libm for every
+            // u = (2k+1) 2^-24 that u01fixedpt<float> can return
+            std::vector<float> tab((size_t)1 << 23);
+            for (uint32_t k = 0; k < (1u << 23); ++k) tab[k] = logf((float)(2u * k + 1u) * 5.9604644775390625e-8f);
+            CREATE_TRY(dmalloc(c, &c->d_logf_tab, tab.size()));
+            CREATE_TRY(cudaMemcpyAsync(c->d_logf_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, c->stream));
+            CREATE_TRY(cudaStreamSynchronize(c->stream));  // `tab` is pageable
+        }
+    }
     CREATE_TRY(cudaStreamSynchronize(c->stream));
 #undef CREATE_TRY
     *out = c;
@@ -360,6 +410,11 @@ muca_status muca_init_chains(muca_ctx *c, uint32_t scheme, uint32_t jack)
         break;
     case MUCA_INIT_ORDERED:
         ia.ordered = 1;
+        break;
+    case MUCA_INIT_MUCA_MAG:  // muca_mag.cpp:64-65
+        ia.key0_mul = 10; ia.key0_jack_mul = 10000; ia.key1 = 0xdecafbadu;
+        ia.ctr0[1] = 100; ia.ctr0[2] = 0xBADCAB1Eu; ia.ctr0[3] = 0xBADC0DEDu;
+        ia.ctr_word = 0;
         break;
     default:
         return fail(c, MUCA_ERR_BAD_ARG, "init scheme %u", scheme);
@@ -440,6 +495,11 @@ static muca_status do_sweep(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint
     if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
     CUDA_TRY(c, cudaSetDevice(c->device));
     if (clear) CUDA_TRY(c, cudaMemsetAsync(c->d_hist, 0, c->hist_len * 8, c->stream));
+    if (c->algo == MUCA_ALGO_RANDOM_SITE) {
+        const RandomArgs a = random_args(c, iter, seed_base, therm, nup);
+        CUDA_TRY(c, launch_sweep_random(a, c->plan.cpb, c->plan.blocks, (int)c->rounds, c->smem_optin, c->stream));
+        return MUCA_OK;
+    }
     const SweepArgs a = sweep_args(c, iter, seed_base, seed_dev_mul, therm, nup);
     CUDA_TRY(c, launch_sweep(c->plan, a, c->stream));
     return MUCA_OK;
@@ -528,7 +588,7 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "weight run needs a weight-mode context");
     if (o->rule > MUCA_UPDATE_RECURSION) return fail(c, MUCA_ERR_BAD_ARG, "rule %u", o->rule);
     if (o->starting_M == 0) return fail(c, MUCA_ERR_BAD_ARG, "starting_M must be >= 1");
-    if (o->nup_schedule > 3) return fail(c, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..3)", o->nup_schedule);
+    if (o->nup_schedule > 4) return fail(c, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..4)", o->nup_schedule);
     CUDA_TRY(c, cudaSetDevice(c->device));
     const auto t0 = std::chrono::steady_clock::now();
     if (o->reinit_chains) {
@@ -550,7 +610,12 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     // the schedule runs at the top of every iteration (:379-382), so a run that
     // starts at full width (a later jack) grows NUPDATES before its first sweep;
     // the device applies it between iterations from then on
-    if (h.st.width == c->N && o->nup_schedule != 2) {
+    if (o->nup_schedule == 4) {
+        // the CPU program multiplies at the top of every iteration, the first included (muca_mag.cpp:131)
+        const unsigned long long nx = (unsigned long long)((double)h.st.nup * 1.05);
+        const uint32_t cap = o->nup_max ? o->nup_max : (1u << 30);
+        h.st.nup = nx > cap ? (cap > h.st.nup ? cap : h.st.nup) : (uint32_t)nx;
+    } else if (h.st.width == c->N && o->nup_schedule != 2) {
         // (schedule 3 knows no histogram yet: it grows like the reference's)
         unsigned long long nx = o->nup_schedule == 1 ? 2ull * h.st.nup : (unsigned)((h.st.nup + 1u) * 1.01);
         const uint32_t cap = o->nup_max ? o->nup_max : (o->nup_schedule == 1 ? (1u << 30) : 0u);
@@ -572,9 +637,12 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     h.rec_cap = (uint32_t)need;
     h.rec_ring = cb ? 1u : 0u;
     CUDA_TRY(c, cudaMemcpyAsync(c->d_ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->stream));
-    const uint64_t therm = o->therm ? o->therm : c->N;  // therm_coeff * N (:315-316)
+    // therm_coeff * N (:315-316); the CPU program's random-site runs thermalise 0 (muca_mag.cpp:140)
+    const uint64_t therm = o->therm ? o->therm : (c->algo == MUCA_ALGO_RANDOM_SITE ? 0 : c->N);
     SweepArgs a = sweep_args(c, 0, 100u, 1000u, therm, 0);  // seed SEED+1000*l (:393)
     a.dyn = &c->d_ctl->st.k;
+    RandomArgs ra = random_args(c, 0, o->jack, therm, 0);  // mcs(..., WORKER, k, mm, 0, NUPDATES)
+    ra.dyn = &c->d_ctl->st.k;
     cudaEvent_t e0, e1, m0, m1;
     CUDA_TRY(c, cudaEventCreate(&e0));
     CUDA_TRY(c, cudaEventCreate(&e1));
@@ -589,7 +657,10 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
         // device decides the schedule and convergence
         cudaError_t e = launch_run_clear(c->d_hist, (uint32_t)c->hist_len, c->d_ctl, c->stream);
         if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
-        if (e == cudaSuccess) e = launch_sweep(c->plan, a, c->stream);
+        if (e == cudaSuccess)
+            e = c->algo == MUCA_ALGO_RANDOM_SITE
+                    ? launch_sweep_random(ra, c->plan.cpb, c->plan.blocks, (int)c->rounds, c->smem_optin, c->stream)
+                    : launch_sweep(c->plan, a, c->stream);
         if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
         if (e == cudaSuccess) e = launch_run_update(c->d_hist, c->d_lnw, c->d_w32, c->d_pacc, c->d_ctl, c->stream,
                                                     c->N, (int)o->rule);

@@ -64,6 +64,24 @@ cudaError_t measure_logf_bracket(float *max_abs_err, cudaStream_t s);
 cudaError_t device_log_eps(int device, cudaStream_t s, double *eps);
 cudaError_t launch_sweep(const SweepPlan &p, const SweepArgs &a, cudaStream_t s);
 
+// Random-site sweep of the reference's CPU weight program (k_sweep_random.cu,
+// muca_mag.cpp:312-393): chain c is WORKER worker0 + c, `seed` the jack
+// index; FP64 weights w[N+1]; logf_tab (2^23 floats, entry k = log of
+// (2k+1) 2^-24) gives the acceptance logarithm, NULL = CUDA's logf.
+struct RandomArgs {
+    uint32_t *lat;
+    int32_t *ej, *edel;
+    const double *w;
+    unsigned long long *hist;
+    uint32_t L, N, WPR, nchains, worker0, seed, iter;
+    unsigned long long therm, nup;
+    const float *logf_tab;
+    const uint32_t *dyn;  // as SweepArgs::dyn
+};
+size_t random_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem);
+cudaError_t launch_sweep_random(const RandomArgs &a, uint32_t cpb, uint32_t blocks, int rounds, size_t smem_optin,
+                                cudaStream_t s);
+
 // Lattice helpers (k_lattice.cu).
 // key = {key0_mul*W + key0_jack_mul*jack + key0_add, key1 + key1_jack_mul*jack}
 struct InitArgs {

@@ -162,9 +162,10 @@ static inline void propose(int8_t *s, const uint32_t *nv, unsigned idx, uint32_t
     *new_s = ns;
 }
 
-/* Acceptance logarithm of the GPU kernels: log(u01fixedpt<float>(r)) on the
- * device is CUDA's logf (muca_delta_multigpu.cu:781,816,
- * produce2_multigpu.cu:446,481).  Without a table this is libm's logf, which
+/* Acceptance logarithm log(u01fixedpt<float>(r)).  The GPU kernels compute
+ * it with CUDA's logf (muca_delta_multigpu.cu:781,816,
+ * produce2_multigpu.cu:446,481), the CPU programs with libm's
+ * (muca_mag.cpp:347,382).  Without a table this is libm's logf, which
  * differs from CUDA's by one ulp for some u; with the table of CUDA's values
  * (tab[k] for u = (2k+1) 2^-24, k = r >> 9, made by devlogf.cu) the decision
  * is the device's. */
@@ -429,7 +430,7 @@ void orc_muca_mag_mcs(unsigned L, unsigned worker, int8_t *s, int32_t *ej, int32
             double diff = -dE * 2 + w[E + dDel] - w[E];
             if (diff >= 0) {
                 s[idx] = (int8_t)ns; energy += dE; E += dDel;
-            } else if (logf(orc_u01fixedpt_f32(r1[i % 4])) < diff) {
+            } else if (accept_logf(r1[i % 4]) < diff) {
                 s[idx] = (int8_t)ns; energy += dE; E += dDel;
             } else {
                 s[idx] = (int8_t)os;
@@ -606,14 +607,28 @@ unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int3
             } else if ((o->sched == 0 || o->sched == 3) && width == N) {
                 const unsigned nu = NUPDATES + 1;
                 nx = (unsigned)(nu * 1.01);
+            } else if (o->sched == 4) {
+                nx = (uint64_t)((double)NUPDATES * 1.05);
+                if (cap == 0) cap = 1u << 30;
             }
             if (cap != 0 && nx > cap) nx = cap > NUPDATES ? cap : NUPDATES;
             NUPDATES = (unsigned)nx;
         }
         total_run += (uint64_t)NUPDATES * o->nchains;
         memset(h, 0, sizeof(uint64_t) * (N + 1));
-        orc_weight_sweep(o->L, 0, o->nchains, lat, ej, edel, w, h, (uint32_t)k, 100u + 1000u * o->gpu, N,
-                         NUPDATES, o->rounds, o->nthreads);
+        if (o->algo == 1) {
+            /* every rank's mcs, then the histogram Reduce (muca_mag.cpp:140-141) */
+            uint64_t *hc = (uint64_t *)malloc(sizeof(uint64_t) * (N + 1));
+            for (unsigned c = 0; c < o->nchains; ++c) {
+                orc_muca_mag_mcs(o->L, c, lat + (size_t)c * N, ej + c, edel + c, lnw, hc, (uint32_t)k, o->jack, 0,
+                                 NUPDATES);
+                for (unsigned i = 0; i <= N; i++) h[i] += hc[i];
+            }
+            free(hc);
+        } else {
+            orc_weight_sweep(o->L, 0, o->nchains, lat, ej, edel, w, h, (uint32_t)k, 100u + 1000u * o->gpu, N,
+                             NUPDATES, o->rounds, o->nthreads);
+        }
         int hs, he;
         orc_hist_range(h, N, &hs, &he);
         unsigned width_temp = (unsigned)(he - hs);
@@ -633,7 +648,9 @@ unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int3
         if (width == N && !reach) reach = 1;
         if (o->flat_minmean ? (mm >= 0.5) : (width == N && dkl < 1e-4)) { *converged = 1; k++; break; }
         if (!o->hold_until_full || width == N) {
-            if (o->recursive) {
+            if (o->recursive == 2) {
+                orc_update_trivial_cpu(h, N, lnw);
+            } else if (o->recursive) {
                 orc_weight_recursion(h, N, p_acc, hs, he, lnw);
                 double tmp = lnw[0];
                 for (unsigned i = 0; i <= N; i++) lnw[i] = lnw[i] - tmp;

@@ -117,7 +117,8 @@ void   orc_observables(double beta, unsigned N, const uint64_t *hist2d, const do
  * k < rec_cap.  Returns the number of iterations run; *converged set. */
 typedef struct orc_weight_opts {
     unsigned L, nchains, jack, gpu, starting_M;
-    int recursive;        /* 0 trivial (GPU flavour), 1 weight_recursion */
+    int recursive;        /* 0 trivial (GPU flavour), 1 weight_recursion, 2 trivial (CPU flavour,
+                             muca_mag.cpp:179-182) */
     int hold_until_full;  /* 0: reference GPU behaviour (always update) */
     int flat_minmean;     /* 0: width==N && D_KL<1e-4 ; 1: min/mean >= 0.5 */
     unsigned max_iter;
@@ -127,7 +128,11 @@ typedef struct orc_weight_opts {
     unsigned sched;       /* NUPDATES schedule: 0 reference ((NUP+1)*1.01 once width==N), 1 doubling
                              once width==N, 2 doubling every iteration from the first, 3 as 0 and
                              doubling once the last histogram had every bin >= 5 % of the mean */
-    unsigned nup_max;     /* cap of NUPDATES: 0 = none for schedule 0, 2^30 for doubling; never decreases */
+    unsigned nup_max;     /* cap of NUPDATES: 0 = none for schedule 0, 2^30 otherwise; never decreases.
+                             Schedule 4: NUP*1.05 every iteration, the first included (muca_mag.cpp:131) */
+    unsigned algo;        /* 0: the GPU weight kernel (sweep order, FP32 weights, therm N);
+                             1: the CPU program's random-site mcs (muca_mag.cpp:312-393) per chain,
+                             WORKER = chain, seed = jack, therm 0, FP64 weights */
 } orc_weight_opts;
 unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int32_t *edel,
                         double *lnw, double *p_acc, double *rec, unsigned rec_cap, int *converged);

@@ -42,7 +42,8 @@ class WeightOpts(C.Structure):
     _fields_ = [("L", C.c_uint), ("nchains", C.c_uint), ("jack", C.c_uint), ("gpu", C.c_uint),
                 ("starting_M", C.c_uint), ("recursive", C.c_int), ("hold_until_full", C.c_int),
                 ("flat_minmean", C.c_int), ("max_iter", C.c_uint), ("rounds", C.c_uint),
-                ("nthreads", C.c_int), ("width_start", C.c_uint), ("sched", C.c_uint), ("nup_max", C.c_uint)]
+                ("nthreads", C.c_int), ("width_start", C.c_uint), ("sched", C.c_uint), ("nup_max", C.c_uint),
+                ("algo", C.c_uint)]
 
 
 def build(ref: bool = False, refgpu: bool = False) -> None:
@@ -164,6 +165,10 @@ def scheme_weight(jack=0, gpu=0):
 
 def scheme_produce(gpu=0):
     return lib().orc_scheme_produce(gpu)
+
+
+def scheme_muca_mag(jack=0):
+    return lib().orc_scheme_muca_mag(jack)
 
 
 def energies(L, lat):
