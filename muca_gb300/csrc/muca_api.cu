@@ -259,7 +259,7 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
         fail(c, MUCA_ERR_BAD_ARG, "kernel=%u (0..3)", p->kernel);
         return bail(MUCA_ERR_BAD_ARG);
     }
-    if ((p->kernel == 2 || p->kernel == 3) && !(p->L % 8 == 0 && p->L >= 8)) {
+    if (p->kernel >= 2 && !(p->L % 8 == 0 && p->L >= 8)) {
         fail(c, MUCA_ERR_BAD_ARG, "kernel %u needs L %% 8 == 0", p->kernel);
         return bail(MUCA_ERR_BAD_ARG);
     }

@@ -37,10 +37,11 @@ __device__ __forceinline__ uint4 philox(uint32_t x0, uint32_t x1, uint32_t x2, u
 {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-        const uint32_t hi0 = __umulhi(kPhiloxM0, x0);
-        const uint32_t lo0 = kPhiloxM0 * x0;
-        const uint32_t hi1 = __umulhi(kPhiloxM1, x2);
-        const uint32_t lo1 = kPhiloxM1 * x2;
+        // one 32x32 -> 64-bit product per multiplier (hi and lo of mulhilo)
+        const unsigned long long p0 = (unsigned long long)kPhiloxM0 * x0;
+        const unsigned long long p1 = (unsigned long long)kPhiloxM1 * x2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
         x0 = hi1 ^ x1 ^ k.a[r];
         x1 = lo1;
         x2 = hi0 ^ x3 ^ k.b[r];

@@ -127,54 +127,57 @@ __device__ __forceinline__ void record_window(uint32_t *__restrict__ histS, unsi
     }
 }
 
-// One full window: the SLOTS same-parity (HALF) sites of word q of row `row`,
-// SLOTS consecutive attempts of the sweep, with packed draws p[].  lat points
-// at this lane's word 0 (stride cpb).  `store` is false for padding lanes:
-// they read another lane's spins, never accept (so their E stays at 2 and
-// every weight index E + dDel_t + dDel_t+1 stays in [0, 4]) and never write.
+// A decoded window: everything its accept/reject scan needs, formed from the
+// lattice words and the packed draws before the scan runs.
+template <int MODE>
+struct WinDec {
+    using WT = typename WeightType<MODE>::T;
+    uint32_t *pc;               // the window's lattice word
+    uint32_t C, ctr, vnib, hs0;  // the word, old and proposed codes (nibbles), parity shift
+    int dE[8], dDel[8], dM[8];
+    WT f2[8];                   // -beta dE as the reference forms it
+    float lf[8];                // __logf(u)
+    uint32_t p[8];              // the packed draws (for the exact replay)
+};
+
+// Decodes the SLOTS same-parity sites (half 0: even, 1: odd) of word q of
+// row `row`, SLOTS consecutive attempts of the sweep, with packed draws p[].
+// lat points at this lane's word 0 (stride cpb).  The half is a value, not a
+// template branch, so decode and scan of neighbouring windows form one basic
+// block the compiler can interleave.
 // BT: -beta*dE comes from the table btab[dE + 8] (any beta) instead of the
 // reference's literal -2 dE (beta = 2); the table holds (float)(-beta*dE),
 // which for beta = 2 is the same value.
-template <int MODE, int SLOTS, int HALF, bool HS = true, bool BT = false>
-__device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
-                                            uint32_t row, uint32_t q, bool rec, bool store, bool checked,
-                                            const typename WeightType<MODE>::T *__restrict__ wS,
-                                            uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
-                                            ChainState &st, const uint32_t (&p)[SLOTS],
-                                            typename WeightType<MODE>::T eps, const float *__restrict__ btab = nullptr)
+template <int MODE, int SLOTS, bool BT = false>
+__device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
+                                              uint32_t row, uint32_t q, uint32_t half, const uint32_t *p,
+                                              const float *__restrict__ btab, WinDec<MODE> &d)
 {
     using WT = typename WeightType<MODE>::T;
     constexpr uint32_t M2 = 0x33333333u, N1 = 0x11111111u;
     const uint32_t rup = (row + 1 == L) ? 0u : row + 1;
     const uint32_t rdn = (row == 0) ? L - 1 : row - 1;
-    uint32_t *pc = lat + (size_t)(row * WPR + q) * cpb;
-    const uint32_t C = *pc;
+    d.pc = lat + (size_t)(row * WPR + q) * cpb;
+    const uint32_t C = *d.pc;
     const uint32_t U = lat[(size_t)(rup * WPR + q) * cpb];
     const uint32_t D = lat[(size_t)(rdn * WPR + q) * cpb];
     // the one neighbour outside word q: left of the first even site, or
     // right of the last odd site (wrapping along the row)
-    uint32_t sq, sb;
-    if (HALF == 0) {
-        sq = q ? q - 1 : (L - 1) >> 4;
-        sb = q ? 15u : ((L - 1) & 15u);
-    } else {
-        sq = (16 * q + 16 < L) ? q + 1 : 0u;
-        sb = 0u;
-    }
+    const uint32_t sq = half ? ((16 * q + 16 < L) ? q + 1 : 0u) : (q ? q - 1 : (L - 1) >> 4);
+    const uint32_t sb = half ? 0u : (q ? 15u : ((L - 1) & 15u));
     const uint32_t sv = spin_code(lat[(size_t)(row * WPR + sq) * cpb], sb);
 
     // Nibble t of `ctr` holds the spin code (s+1) of the window's site t;
-    // nibble t of `nbs` the sum of its four neighbours' codes (0..8, no carries).
-    uint32_t ctr, nbs;
-    if (HALF == 0) {
-        const uint32_t oc = (C >> 2) & M2;  // odd sites: right neighbours, shifted: left ones
-        ctr = C & M2;
-        nbs = oc + ((oc << 4) | sv) + (U & M2) + (D & M2);
-    } else {
-        const uint32_t ec = C & M2;  // even sites: left neighbours, shifted: right ones
-        ctr = (C >> 2) & M2;
-        nbs = ec + ((ec >> 4) | (sv << (4 * (SLOTS - 1)))) + ((U >> 2) & M2) + ((D >> 2) & M2);
-    }
+    // nibble t of `nbs` the sum of its four neighbours' codes (0..8, no
+    // carries).  `oth` holds the other parity's codes: for even sites the
+    // right neighbours (shifted up: the left ones, with sv entering at t=0),
+    // for odd sites the left neighbours (shifted down: the right ones, sv at
+    // the top).
+    const uint32_t hs0 = half ? 2u : 0u;
+    const uint32_t ctr = (C >> hs0) & M2;
+    const uint32_t oth = (C >> (2u - hs0)) & M2;
+    const uint32_t side = half ? ((oth >> 4) | (sv << (4 * (SLOTS - 1)))) : ((oth << 4) | sv);
+    const uint32_t nbs = oth + side + ((U >> hs0) & M2) + ((D >> hs0) & M2);
     // Proposals of all sites at once, nibble-parallel:  s -> s +/- 1 with the
     // cyclic wrap is code -> (code + 1 + d) mod 3, d the direction bit.
     uint32_t dn = 0;
@@ -187,21 +190,35 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
     const uint32_t nzn = ((vnib ^ N1) | ((vnib ^ N1) >> 1)) & N1;  // s_new != 0
     const uint32_t ddb = nzn + N1 - nzo;                           // dDel + 1 (0..2)
     const uint32_t dvb = vnib + 0x22222222u - ctr;                 // s_new - s_old + 2 (0..4)
-
-    int dE[SLOTS], dDel[SLOTS], dM[SLOTS];
-    WT f2[SLOTS];
-    float lf[SLOTS];
+    d.C = C;
+    d.ctr = ctr;
+    d.vnib = vnib;
+    d.hs0 = hs0;
 #pragma unroll
     for (int t = 0; t < SLOTS; ++t) {
         const int dv = (int)((dvb >> (4 * t)) & 7u) - 2;
-        dDel[t] = (int)((ddb >> (4 * t)) & 3u) - 1;
-        dE[t] = dv * (4 - (int)((nbs >> (4 * t)) & 15u));  // -(s_new - s_old) * (sum of neighbour spins)
-        dM[t] = dv;
-        if (BT) f2[t] = (WT)btab[dE[t] + 8];
-        else    f2[t] = (WT)(-2 * dE[t]);
-        lf[t] = __logf(u01f(p[t]));
+        d.dDel[t] = (int)((ddb >> (4 * t)) & 3u) - 1;
+        d.dE[t] = dv * (4 - (int)((nbs >> (4 * t)) & 15u));  // -(s_new - s_old) * (sum of neighbour spins)
+        d.dM[t] = dv;
+        if (BT) d.f2[t] = (WT)btab[d.dE[t] + 8];
+        else    d.f2[t] = (WT)(-2 * d.dE[t]);
+        d.lf[t] = __logf(u01f(p[t]));
+        d.p[t] = p[t];
     }
+}
 
+// The accept/reject scan of a decoded window, its lattice write and its
+// histogram entries.  `store` is false for padding lanes: they read another
+// lane's spins, never accept (so their E stays at 2 and every weight index
+// E + dDel_t + dDel_t+1 stays in [0, 4]) and never write.
+template <int MODE, int SLOTS, bool HS = true>
+__device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, bool store, bool checked,
+                                            const typename WeightType<MODE>::T *__restrict__ wS,
+                                            uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
+                                            ChainState &st, typename WeightType<MODE>::T eps)
+{
+    using WT = typename WeightType<MODE>::T;
+    constexpr uint32_t M2 = 0x33333333u;
     // Sequential accept/reject over E_Delta:
     //   accept  <=>  diff >= 0  ||  logf(u) < diff,
     //   diff = (float)(-2 dE) + w[E + dDel] - w[E]   (muca_delta_multigpu.cu:810-816)
@@ -213,11 +230,11 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
     const ChainState s0 = st;
     const WT wE0 = wS[st.E];
     WT wE = wE0;
-    WT A = wS[st.E + dDel[0]];
+    WT A = wS[st.E + d.dDel[0]];
     WT c0 = A, c1 = A;
     if (SLOTS > 1) {
-        c0 = wS[st.E + dDel[1]];
-        c1 = wS[st.E + dDel[0] + dDel[1]];
+        c0 = wS[st.E + d.dDel[1]];
+        c1 = wS[st.E + d.dDel[0] + d.dDel[1]];
     }
     uint32_t accm = 0;
     bool near = false;
@@ -226,16 +243,16 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
     for (int t = 0; t < SLOTS; ++t) {
         WT diff;
         if (MODE == kModeWeight)
-            diff = __fsub_rn(__fadd_rn((float)f2[t], (float)A), (float)wE);
+            diff = __fsub_rn(__fadd_rn((float)d.f2[t], (float)A), (float)wE);
         else
-            diff = __dsub_rn(__dadd_rn((double)f2[t], (double)A), (double)wE);
-        const WT l = (WT)lf[t];
+            diff = __dsub_rn(__dadd_rn((double)d.f2[t], (double)A), (double)wE);
+        const WT l = (WT)d.lf[t];
         const bool acc = store && ((diff >= (WT)0) || (l < diff));
         near |= (diff < (WT)0) && (fabs(l - diff) <= eps);
         if (acc) {
-            st.E += dDel[t];
-            st.EJ += dE[t];
-            st.M += dM[t];
+            st.E += d.dDel[t];
+            st.EJ += d.dE[t];
+            st.M += d.dM[t];
             wE = A;
             accm |= 0xFu << (4 * t);
         }
@@ -244,8 +261,8 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
         if (t + 1 < SLOTS) {
             A = acc ? c1 : c0;
             if (t + 2 < SLOTS) {
-                c0 = wS[st.E + dDel[t + 2]];
-                c1 = wS[st.E + dDel[t + 1] + dDel[t + 2]];
+                c0 = wS[st.E + d.dDel[t + 2]];
+                c1 = wS[st.E + d.dDel[t + 1] + d.dDel[t + 2]];
             }
         }
     }
@@ -255,19 +272,19 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
         accm = 0;
 #pragma unroll
         for (int t = 0; t < SLOTS; ++t) {
-            const WT wn = wS[st.E + dDel[t]];
+            const WT wn = wS[st.E + d.dDel[t]];
             WT diff;
             if (MODE == kModeWeight)
-                diff = __fsub_rn(__fadd_rn((float)f2[t], (float)wn), (float)wE);
+                diff = __fsub_rn(__fadd_rn((float)d.f2[t], (float)wn), (float)wE);
             else
-                diff = __dsub_rn(__dadd_rn((double)f2[t], (double)wn), (double)wE);
+                diff = __dsub_rn(__dadd_rn((double)d.f2[t], (double)wn), (double)wE);
             bool acc = diff >= (WT)0;
-            if (!acc) acc = (WT)logf(u01f(p[t])) < diff;
+            if (!acc) acc = (WT)logf(u01f(d.p[t])) < diff;
             acc = acc && store;
             if (acc) {
-                st.E += dDel[t];
-                st.EJ += dE[t];
-                st.M += dM[t];
+                st.E += d.dDel[t];
+                st.EJ += d.dE[t];
+                st.M += d.dM[t];
                 wE = wn;
                 accm |= 0xFu << (4 * t);
             }
@@ -275,9 +292,24 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
             Ms[t] = st.M;
         }
     }
-    const uint32_t merged = (ctr & ~accm) | (vnib & accm);
-    if (store) *pc = (HALF == 0) ? ((C & ~M2) | merged) : ((C & M2) | (merged << 2));
+    const uint32_t merged = (d.ctr & ~accm) | (d.vnib & accm);
+    if (store) *d.pc = (d.C & (d.hs0 ? M2 : ~M2)) | (merged << d.hs0);
     if (rec) record_window<MODE, SLOTS, HS>(histS, histG, Es, Ms, checked);
+}
+
+// One full window: decode, then scan.
+template <int MODE, int SLOTS, int HALF, bool HS = true, bool BT = false>
+__device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
+                                            uint32_t row, uint32_t q, bool rec, bool store, bool checked,
+                                            const typename WeightType<MODE>::T *__restrict__ wS,
+                                            uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
+                                            ChainState &st, const uint32_t (&p)[SLOTS],
+                                            typename WeightType<MODE>::T eps, const float *__restrict__ btab = nullptr,
+                                            uint32_t hrt = 0)
+{
+    WinDec<MODE> d;
+    decode_window<MODE, SLOTS, BT>(lat, cpb, L, WPR, row, q, HALF < 0 ? hrt : (uint32_t)HALF, p, btab, d);
+    scan_window<MODE, SLOTS, HS>(d, rec, store, checked, wS, histS, histG, st, eps);
 }
 
 // The first `len` (< window size) attempts of a window, one at a time as
@@ -470,15 +502,15 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
 #pragma unroll
             for (int t = 0; t < 8; ++t) p[t] = next[t];
             advance(2);  // independent of the window below: overlaps its scan
-            if (half) window_core<MODE, 8, 1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, btab);
-            else      window_core<MODE, 8, 0, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, btab);
+            window_core<MODE, 8, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p,
+                                             eps, btab, half);
         } else {
             uint32_t p[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) p[t] = next[t];
             advance(1);
-            if (half) window_core<MODE, 4, 1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, btab);
-            else      window_core<MODE, 4, 0, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, btab);
+            window_core<MODE, 4, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p,
+                                             eps, btab, half);
         }
         return true;
     });
@@ -494,5 +526,6 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
     __syncthreads();
     if (HS) drain_hist<MODE>(histS, a.hist, a.N);
 }
+
 
 }  // namespace muca
