@@ -17,9 +17,11 @@ weight update on the device.  Spins start from the reference initialisation
   roofline      HBM form: 1.5 algorithmic bytes per attempt (2-bit spins:
                 site read + write, 4 neighbour reads) over the sweep kernel's
                 event time, against the measured copy bandwidth;
-  roofline_int  the bound that applies (lattice resident in shared memory):
-                0.5 Philox4x32-7 blocks per attempt against the measured
+  roofline_int  0.5 Philox4x32-7 blocks per attempt against the measured
                 Philox block rate of this GPU (muca_philox_peak);
+  roofline_issue  warp instructions per launch (ncu, committed profile)
+                over the launch time against 4 per clock per SM: the bound
+                that applies (lattice resident in shared memory);
   cpu_baseline  the CPU oracle (the reference algorithm restated in C, one
                 chain per thread task, all host threads) on full steps.
 
@@ -137,6 +139,21 @@ def profile_traffic():
         return d
     except (OSError, ValueError):
         return None
+
+
+def issue_roofline(prof, sweep_s, clk, sms):
+    """Instruction issue of the sweep: warp instructions per launch (ncu,
+    the committed profile of this workload) over the launch's event time,
+    against one warp instruction per clock per SM sub-partition (4 per SM)
+    at the SM clock sampled during the timed region."""
+    if not prof or not prof.get("warp_instructions_per_launch"):
+        return None
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    achieved = prof["warp_instructions_per_launch"] / sweep_s
+    peak = 4.0 * sms * mhz * 1e6
+    return {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "G warp instructions/s",
+            "frac": achieved / peak, "peak_source": "4 warp instructions/clock/SM at the sampled SM clock",
+            "instructions_source": prof.get("source")}
 
 
 def cpu_oracle_rate(L, chains, nthreads, min_seconds=12.0, max_reps=200):
@@ -327,6 +344,7 @@ def ours_arm(args, ws, rank, local):
                              "peak": philox_peak / 1e9, "unit": "G Philox4x32-7 blocks/s",
                              "frac": PHILOX_BLOCKS_PER_ATTEMPT * att_rate / philox_peak,
                              "peak_source": "measured (muca_philox_peak on this GPU)"},
+            "roofline_issue": issue_roofline(prof, sweep_avg, clk, eng.info.sms),
             "sweep_ms": 1e3 * sweep_avg, "gpu_launches": 2 * args.steps,
             "clocks": clk, "wall_s_timed_region": t_wall,
         }
