@@ -443,7 +443,24 @@ def production_metric(local):
             e.observables(2.0, 1.96)
         t_obs = (time.perf_counter() - t0) / reps
     bins = (N + 1) * (N + 2) // 2
+    ref = None
+    try:  # the reference production kernel on the same lattice and step
+        from oracle import orc
+        orc.build(refgpu=True)
+        if orc.refgpu() is not None:
+            with m.Engine(L, nchains=nc, device=local, mode=m.MODE_PRODUCE) as e2:
+                e2.init_chains(m.INIT_PRODUCE, 0)
+                lat0 = e2.get_lattice()
+            z = np.zeros(nc, np.int32)
+            w64 = np.zeros(N + 1)
+            lat1, _, ej, ed, mg, _ = orc.refgpu_produce(L, lat0, w64, z, z, z, 0, 100, N, 0, compute_energies=True)
+            _, _, _, _, _, ms = orc.refgpu_produce(L, lat1, w64, ej, ed, mg, 1, 100, 0, sweeps * N)
+            ref = {"value": nc * sweeps * N / (ms * 1e6), "ms": ms,
+                   "kernel": "produce2_multigpu.cu mcs, compiled for sm_103a, same lattice, weights and step"}
+    except Exception as ex:
+        ref = {"unavailable": str(ex)[:200]}
     return {"metric": "production sweep attempts/ns at L=128", "value": nc * sweeps * N / (t_sweep * 1e9),
+            "ref_gpu_kernel": ref,
             "unit": "attempts/ns", "chains": nc, "sweeps": sweeps, "timing": "CUDA events around one launch",
             "reweighting": {"bins": bins, "ms": 1e3 * t_obs, "GB_per_s": 8 * bins / t_obs / 1e9,
                             "timing": "host clock, mean of %d calls (histogram read once per call)" % reps}}

@@ -114,7 +114,12 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
     WT *wS;
     uint32_t *histS, *gl;
     const size_t lat_off = ring_off + smem_ring_bytes(P);
-    uint32_t *lat = prologue<MODE, LAT_SMEM>(a, smem, lat_off, cpb, producer ? 0xFFFFFFFFu : lane, blockIdx.x, wS, histS, gl);
+    constexpr bool DT = MODE == kModeProduce;  // production scans on the FP32 difference table
+    float tol = 0.0f;
+    uint32_t *lat = prologue<MODE, LAT_SMEM, true, DT>(a, smem, lat_off, cpb, producer ? 0xFFFFFFFFu : lane,
+                                                       blockIdx.x, wS, histS, gl, &tol);
+    const double *wG = reinterpret_cast<const double *>(a.w);
+    const WT *wP = DT ? reinterpret_cast<const WT *>(a.w) : wS;
     __syncthreads();
     ChainSetup<MODE, R> cs;
     cs.init(a, cpb, lane, blockIdx.x);
@@ -158,21 +163,21 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
 #pragma unroll
                 for (int t = 0; t < 8; ++t) p[t] = slot[t * 32];
                 mbar_arrive(empty + s);
-                partial_core<MODE>(lat, cpb, L, WPR, row, q, half, len, rec, store, wS, histS, a.hist, st, p);
+                partial_core<MODE>(lat, cpb, L, WPR, row, q, half, len, rec, store, wP, histS, a.hist, st, p);
             } else if (cnt == 8) {
                 uint32_t p[8];
 #pragma unroll
                 for (int t = 0; t < 8; ++t) p[t] = slot[t * 32];
                 mbar_arrive(empty + s);
-                if (half) window_core<MODE, 8, 1>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps);
-                else      window_core<MODE, 8, 0>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps);
+                if (half) window_core<MODE, 8, 1>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, nullptr, 0, wG, tol);
+                else      window_core<MODE, 8, 0>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, nullptr, 0, wG, tol);
             } else {
                 uint32_t p[4];
 #pragma unroll
                 for (int t = 0; t < 4; ++t) p[t] = slot[t * 32];
                 mbar_arrive(empty + s);
-                if (half) window_core<MODE, 4, 1>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps);
-                else      window_core<MODE, 4, 0>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps);
+                if (half) window_core<MODE, 4, 1>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, nullptr, 0, wG, tol);
+                else      window_core<MODE, 4, 0>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, nullptr, 0, wG, tol);
             }
             ++w;
             return true;

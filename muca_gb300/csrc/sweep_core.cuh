@@ -135,7 +135,7 @@ struct WinDec {
     uint32_t *pc;               // the window's lattice word
     uint32_t C, ctr, vnib, hs0;  // the word, old and proposed codes (nibbles), parity shift
     int dE[8], dDel[8], dM[8];
-    WT f2[8];                   // -beta dE as the reference forms it
+    float f2[8];                // -beta dE (an even integer for beta = 2: exact in FP32 and FP64)
     float lf[8];                // __logf(u)
     uint32_t p[8];              // the packed draws (for the exact replay)
 };
@@ -200,8 +200,8 @@ __device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32
         d.dDel[t] = (int)((ddb >> (4 * t)) & 3u) - 1;
         d.dE[t] = dv * (4 - (int)((nbs >> (4 * t)) & 15u));  // -(s_new - s_old) * (sum of neighbour spins)
         d.dM[t] = dv;
-        if (BT) d.f2[t] = (WT)btab[d.dE[t] + 8];
-        else    d.f2[t] = (WT)(-2 * d.dE[t]);
+        if (BT) d.f2[t] = btab[d.dE[t] + 8];
+        else    d.f2[t] = (float)(-2 * d.dE[t]);
         d.lf[t] = __logf(u01f(p[t]));
         d.p[t] = p[t];
     }
@@ -215,10 +215,77 @@ template <int MODE, int SLOTS, bool HS = true>
 __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, bool store, bool checked,
                                             const typename WeightType<MODE>::T *__restrict__ wS,
                                             uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
-                                            ChainState &st, typename WeightType<MODE>::T eps)
+                                            ChainState &st, typename WeightType<MODE>::T eps,
+                                            const double *__restrict__ wG = nullptr, float tol = 0.0f)
 {
     using WT = typename WeightType<MODE>::T;
     constexpr uint32_t M2 = 0x33333333u;
+    if (MODE == kModeProduce) {
+        // Production: the reference forms diff in FP64 (produce2_multigpu.cu:474),
+        // and FP64 issues slowly on this GPU.  The scan runs in FP32 on the
+        // staged differences T[E] (prologue<..., DT>): fast = f2 + T[E].dDel,
+        // within `tol` of the FP64 diff.  Any lane where that leaves the
+        // decision in doubt sends the warp to the exact FP64 replay of the
+        // window, with the FP64 weights in global memory, so every decision
+        // is the reference's.
+        const float2 *T = reinterpret_cast<const float2 *>(wS);
+        const ChainState s0 = st;
+        const float epsf = (float)eps;
+        float2 tE = T[st.E];
+        float2 tN = T[st.E + d.dDel[0]];
+        uint32_t accm = 0;
+        bool near = false;
+        int Es[SLOTS], Ms[SLOTS];
+#pragma unroll
+        for (int t = 0; t < SLOTS; ++t) {
+            const int dd = d.dDel[t];
+            const float dl = dd == 0 ? 0.0f : (dd < 0 ? tE.x : tE.y);
+            const float fast = __fadd_rn(d.f2[t], dl);
+            const float l = d.lf[t];
+            const bool acc = store && ((fast >= 0.0f) || (l < fast));
+            // With a zero difference (dDel = 0, or equal neighbouring weights)
+            // fast is f2 itself and the FP64 diff is f2 + e with
+            // |e| <= 2^-53 (|w| + 16): the same sign, and a zero f2 leaves
+            // diff >= 0 or a negative diff that every logf(u) < 0 clears --
+            // accepted either way.  Only a nonzero difference can put the
+            // sign in doubt; the comparison with log(u) is in doubt when
+            // __logf(u) lies within tol + eps of fast.
+            near |= ((dl != 0.0f) && (fabsf(fast) <= tol)) || ((fast < 0.0f) && (fabsf(l - fast) <= tol + epsf));
+            if (acc) {
+                st.E += dd;
+                st.EJ += d.dE[t];
+                st.M += d.dM[t];
+                tE = tN;
+                accm |= 0xFu << (4 * t);
+            }
+            Es[t] = st.E;
+            Ms[t] = st.M;
+            if (t + 1 < SLOTS) tN = T[st.E + d.dDel[t + 1]];
+        }
+        if (__any_sync(0xffffffffu, near)) {
+            st = s0;
+            accm = 0;
+#pragma unroll
+            for (int t = 0; t < SLOTS; ++t) {
+                const double diff = __dsub_rn(__dadd_rn((double)d.f2[t], wG[st.E + d.dDel[t]]), wG[st.E]);
+                bool acc = diff >= 0.0;
+                if (!acc) acc = (double)logf(u01f(d.p[t])) < diff;
+                acc = acc && store;
+                if (acc) {
+                    st.E += d.dDel[t];
+                    st.EJ += d.dE[t];
+                    st.M += d.dM[t];
+                    accm |= 0xFu << (4 * t);
+                }
+                Es[t] = st.E;
+                Ms[t] = st.M;
+            }
+        }
+        const uint32_t merged = (d.ctr & ~accm) | (d.vnib & accm);
+        if (store) *d.pc = (d.C & (d.hs0 ? M2 : ~M2)) | (merged << d.hs0);
+        if (rec) record_window<MODE, SLOTS, HS>(histS, histG, Es, Ms, checked);
+        return;
+    }
     // Sequential accept/reject over E_Delta:
     //   accept  <=>  diff >= 0  ||  logf(u) < diff,
     //   diff = (float)(-2 dE) + w[E + dDel] - w[E]   (muca_delta_multigpu.cu:810-816)
@@ -305,11 +372,12 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
                                             uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
                                             ChainState &st, const uint32_t (&p)[SLOTS],
                                             typename WeightType<MODE>::T eps, const float *__restrict__ btab = nullptr,
-                                            uint32_t hrt = 0)
+                                            uint32_t hrt = 0, const double *__restrict__ wG = nullptr,
+                                            float tol = 0.0f)
 {
     WinDec<MODE> d;
     decode_window<MODE, SLOTS, BT>(lat, cpb, L, WPR, row, q, HALF < 0 ? hrt : (uint32_t)HALF, p, btab, d);
-    scan_window<MODE, SLOTS, HS>(d, rec, store, checked, wS, histS, histG, st, eps);
+    scan_window<MODE, SLOTS, HS>(d, rec, store, checked, wS, histS, histG, st, eps, wG, tol);
 }
 
 // The first `len` (< window size) attempts of a window, one at a time as
@@ -358,10 +426,15 @@ __device__ __noinline__ void partial_core(uint32_t *__restrict__ lat, uint32_t c
 // Stage weights, clear the histogram, stage this block's lattice; returns
 // the lane's lattice base (shared or global).  Only lanes < cpb copy.
 // `blk` is the chain block (blockIdx.x for a single simulation).
-template <int MODE, bool LAT_SMEM, bool HS = true>
+// DT (production): instead of the FP64 weights, shared memory holds the
+// FP32 differences T[E] = {w[E-1] - w[E], w[E+1] - w[E]} of the FP64 weights
+// (same size), and *tol gets the bound of the FP32 fast test (see
+// scan_window); the FP64 weights stay in global memory for the exact test.
+template <int MODE, bool LAT_SMEM, bool HS = true, bool DT = false>
 __device__ __forceinline__ uint32_t *prologue(const SweepArgs &a, unsigned char *smem, size_t lat_offset,
                                               uint32_t cpb, uint32_t lane, uint32_t blk,
-                                              typename WeightType<MODE>::T *&wS, uint32_t *&histS, uint32_t *&gl)
+                                              typename WeightType<MODE>::T *&wS, uint32_t *&histS, uint32_t *&gl,
+                                              float *tol = nullptr)
 {
     using WT = typename WeightType<MODE>::T;
     const uint32_t N = a.N, nt = blockDim.x, tid = threadIdx.x;
@@ -369,7 +442,41 @@ __device__ __forceinline__ uint32_t *prologue(const SweepArgs &a, unsigned char 
     histS = reinterpret_cast<uint32_t *>(smem + smem_weights_bytes(MODE, N));
     uint32_t *latS = reinterpret_cast<uint32_t *>(smem + lat_offset);
     const WT *wg = reinterpret_cast<const WT *>(a.w);
-    for (uint32_t i = tid; i <= N; i += nt) wS[i] = wg[i];
+    if (MODE == kModeProduce && DT) {
+        __shared__ float s_md[32];
+        __shared__ double s_mw[32];
+        float2 *T = reinterpret_cast<float2 *>(smem);
+        const double *w64 = reinterpret_cast<const double *>(a.w);
+        float md = 0.0f;
+        double mw = 0.0;
+        for (uint32_t i = tid; i <= N; i += nt) {
+            const double w0 = w64[i];
+            const float dm = i > 0 ? (float)__dsub_rn(w64[i - 1], w0) : 0.0f;
+            const float dp = i < N ? (float)__dsub_rn(w64[i + 1], w0) : 0.0f;
+            T[i] = make_float2(dm, dp);
+            md = fmaxf(md, fmaxf(fabsf(dm), fabsf(dp)));
+            mw = fmax(mw, fabs(w0));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
+            mw = fmax(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+        }
+        if ((tid & 31u) == 0) { s_md[tid >> 5] = md; s_mw[tid >> 5] = mw; }
+        __syncthreads();
+        if (tid == 0) {
+            for (uint32_t k = 1; k < (nt + 31) / 32; ++k) { md = fmaxf(md, s_md[k]); mw = fmax(mw, s_mw[k]); }
+            // |fast - exact| <= 2^-24 (|T| + |fast|) + 2^-53 (|w| + 16 + |diff| + |T|), |T| <= md,
+            // |fast|, |diff| <= 16 + md; twice that
+            const double m = (double)md * 1.0001;
+            s_md[0] = (float)((2.0 * 5.9604644775390625e-8 * (2.0 * m + 16.0) +
+                               2.0 * 1.1102230246251565e-16 * (mw + 32.0 + 2.0 * m)) * 1.0001);
+        }
+        __syncthreads();
+        if (tol) *tol = s_md[0];
+    } else {
+        for (uint32_t i = tid; i <= N; i += nt) wS[i] = wg[i];
+    }
     if (MODE == kModeWeight && HS)
         for (uint32_t i = tid; i <= N; i += nt) histS[i] = 0u;
     const uint32_t words = a.L * a.WPR;
@@ -462,8 +569,13 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
     WT *wS;
     uint32_t *histS, *gl;
     const size_t lat_off = smem_weights_bytes(MODE, a.N) + (HS ? smem_hist_bytes(MODE, a.N) : 0);
-    uint32_t *lat = prologue<MODE, LAT_SMEM, HS>(a, smem, lat_off, cpb, lane, blk, wS, histS, gl);
+    constexpr bool DT = MODE == kModeProduce;  // production scans on the FP32 difference table
+    float tol = 0.0f;
+    uint32_t *lat = prologue<MODE, LAT_SMEM, HS, DT>(a, smem, lat_off, cpb, lane, blk, wS, histS, gl, &tol);
     __syncthreads();
+    const double *wG = reinterpret_cast<const double *>(a.w);
+    // the step-by-step path reads the weights it needs: FP64 ones from global memory in production
+    const WT *wP = DT ? reinterpret_cast<const WT *>(a.w) : wS;
     ChainSetup<MODE, R> cs;
     cs.init(a, cpb, lane, blk);
     const bool store = lane < cpb;
@@ -495,7 +607,7 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
                                               bool rec_phase) {
         const bool rec = rec_phase && cs.active;
         if (len < cnt) {
-            partial_core<MODE, HS, BT>(lat, cpb, L, WPR, row, q, half, len, rec, store, wS, histS, a.hist, st, next, btab);
+            partial_core<MODE, HS, BT>(lat, cpb, L, WPR, row, q, half, len, rec, store, wP, histS, a.hist, st, next, btab);
             advance((len + 3u) >> 2);
         } else if (cnt == 8) {
             uint32_t p[8];
@@ -503,14 +615,14 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
             for (int t = 0; t < 8; ++t) p[t] = next[t];
             advance(2);  // independent of the window below: overlaps its scan
             window_core<MODE, 8, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p,
-                                             eps, btab, half);
+                                             eps, btab, half, wG, tol);
         } else {
             uint32_t p[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) p[t] = next[t];
             advance(1);
             window_core<MODE, 4, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p,
-                                             eps, btab, half);
+                                             eps, btab, half, wG, tol);
         }
         return true;
     });
