@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ref-gpu", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the flat-run, batch and production lines")
+    p.add_argument("--only", choices=["flat_run", "batch", "production"],
+                   help="run only this extra line and print it (for profiling a smaller case)")
+    p.add_argument("--production-L", type=int, default=128, help="lattice size of --only production")
     p.add_argument("--kernel", type=int, default=0, help="sweep kernel: 0 auto, 1 generic, 2 windowed, 3 specialised")
     return p.parse_args()
 
@@ -414,14 +417,14 @@ def batch_metric(local, iters=32):
             "graph": "%d iterations (clear, persistent sweep, update) per CUDA graph" % iters}
 
 
-def production_metric(local):
+def production_metric(local, L=128, with_ref=True):
     """Production at L=128, 16384 chains (the L=128 configuration's shapes,
     with the sweep counts scaled down): FP64 weights, 2D (E_Delta, M) u64
     histogram of 134 M bins; then the reweighting of that histogram."""
     import numpy as np
     import torch
     import muca_gb300 as m
-    L, nc = 128, 16384
+    nc = 16384
     N = L * L
     stream = torch.cuda.Stream()
     with m.Engine(L, nchains=nc, device=local, mode=m.MODE_PRODUCE, stream=stream.cuda_stream) as e:
@@ -445,6 +448,8 @@ def production_metric(local):
     bins = (N + 1) * (N + 2) // 2
     ref = None
     try:  # the reference production kernel on the same lattice and step
+        if not with_ref:
+            raise RuntimeError("not requested")
         from oracle import orc
         orc.build(refgpu=True)
         if orc.refgpu() is not None:
@@ -459,7 +464,7 @@ def production_metric(local):
                    "kernel": "produce2_multigpu.cu mcs, compiled for sm_103a, same lattice, weights and step"}
     except Exception as ex:
         ref = {"unavailable": str(ex)[:200]}
-    return {"metric": "production sweep attempts/ns at L=128", "value": nc * sweeps * N / (t_sweep * 1e9),
+    return {"metric": "production sweep attempts/ns at L=%d" % L, "value": nc * sweeps * N / (t_sweep * 1e9),
             "ref_gpu_kernel": ref,
             "unit": "attempts/ns", "chains": nc, "sweeps": sweeps, "timing": "CUDA events around one launch",
             "reweighting": {"bins": bins, "ms": 1e3 * t_obs, "GB_per_s": 8 * bins / t_obs / 1e9,
@@ -501,6 +506,15 @@ def main():
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return reference_arm(args, ws, rank)
+    if args.only:
+        import torch
+        torch.cuda.set_device(local)
+        from muca_gb300 import build as b
+        b.build()
+        fn = {"flat_run": flat_run_metric, "batch": batch_metric,
+              "production": lambda d: production_metric(d, args.production_L, with_ref=False)}[args.only]
+        print(json.dumps(fn(local)))
+        return 0
     return ours_arm(args, ws, rank, local)
 
 

@@ -9,10 +9,10 @@
 // m = -i, -i+2, ..., i at (i^2 + 2i + m)/2 = i(i+1)/2 + (m+i)/2.
 //
 // The sums stream the u64 histogram once (HBM bound at 8 B per bin), one
-// warp per row; empty bins cost no FP64 work.  Each term is formed as the reference forms it:
-// (double)(|m| H) * boltz_i, (double)(m^2 H) * boltz_i; partial sums are
-// combined per warp, per block and then in a fixed-order second pass, so the
-// result is deterministic and agrees with the long-double host sum to ~1e-15.
+// warp per row, with exact integer moments per row (see k_observables);
+// the per-row FP64 terms are combined per warp, per block and then in a
+// fixed-order second pass, so the result is deterministic and agrees with
+// the long-double host sum to ~1e-15.
 #include "muca_device.cuh"
 #include "muca_internal.h"
 
@@ -49,10 +49,29 @@ __global__ void k_weight_shift(double *lnw, uint32_t N, double beta, double delt
 
 // One warp per row of the triangle at a time (row i = E_Delta holds the i+1
 // bins m = -i, -i+2, ..., i from b = i(i+1)/2): the lanes stream the row's
-// u64 counts with coalesced loads, kObsUnroll independent loads per lane in
-// flight, and boltz_i is formed once per row.  Warp w takes rows w, w + W,
-// w + 2W, ... (W warps in the grid), which spreads the long rows evenly.
+// u64 counts with coalesced loads, 2 kObsUnroll independent loads per lane
+// in flight (double-buffered).  Within a row boltz_i is a common factor, so the lanes sum
+// H, |m| H, m^2 H and m^4 H exactly in 128-bit integers (integer pipes; FP64
+// issues slowly on this GPU), the warp reduces them, and lane 0 adds
+// sum_k(i) * boltz_i to its FP64 accumulators: one FP64 product per row and
+// moment instead of one per bin.  Warp w takes rows w, w + W, w + 2W, ...
+// (W warps in the grid), which spreads the long rows evenly.
 constexpr int kObsUnroll = 8;
+
+typedef unsigned __int128 u128;
+
+__device__ __forceinline__ u128 shfl_xor_u128(u128 v, int o)
+{
+    const unsigned long long lo = __shfl_xor_sync(0xffffffffu, (unsigned long long)v, o);
+    const unsigned long long hi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(v >> 64), o);
+    return ((u128)hi << 64) | lo;
+}
+
+__device__ __forceinline__ double u128_to_double(u128 v)
+{
+    return __dadd_rn(__dmul_rn((double)(unsigned long long)(v >> 64), 18446744073709551616.0),
+                     (double)(unsigned long long)v);
+}
 
 __global__ void __launch_bounds__(kObsThreads) k_observables(const unsigned long long *__restrict__ hist,
                                                              const double *__restrict__ lnw, uint32_t N,
@@ -65,27 +84,47 @@ __global__ void __launch_bounds__(kObsThreads) k_observables(const unsigned long
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i <= N; i += nwarps) {
         const unsigned long long *row = hist + (unsigned long long)i * (i + 1) / 2;
-        const double bz = exp(__dsub_rn(__dmul_rn(nbd, (double)i), lnw[i]));
+        u128 a0 = 0, a1 = 0, a2 = 0, a4 = 0;
+        // double-buffered: the next chunk's loads are in flight while this one is summed
+        unsigned long long h[kObsUnroll], hn[kObsUnroll];
+#pragma unroll
+        for (int k = 0; k < kObsUnroll; ++k) {
+            const uint32_t j = ln + 32u * k;
+            h[k] = j <= i ? __ldcs(row + j) : 0ull;
+        }
         for (uint32_t j0 = 0; j0 <= i; j0 += 32u * kObsUnroll) {
-            unsigned long long h[kObsUnroll];
 #pragma unroll
             for (int k = 0; k < kObsUnroll; ++k) {
-                const uint32_t j = j0 + ln + 32u * k;
-                h[k] = j <= i ? __ldcs(row + j) : 0ull;
+                const uint32_t j = j0 + 32u * kObsUnroll + ln + 32u * k;
+                hn[k] = j <= i ? __ldcs(row + j) : 0ull;
             }
 #pragma unroll
             for (int k = 0; k < kObsUnroll; ++k) {
                 const unsigned long long H = h[k];
-                if (H == 0) continue;
                 const int m = 2 * (int)(j0 + ln + 32u * k) - (int)i;
-                const unsigned long long am = (unsigned long long)(m < 0 ? -m : m);
-                const double t0 = __dmul_rn((double)H, bz);
-                const double t2 = __dmul_rn((double)(am * am * H), bz);
-                s0 = __dadd_rn(s0, t0);
-                s1 = __dadd_rn(s1, __dmul_rn((double)(am * H), bz));
-                s2 = __dadd_rn(s2, t2);
-                s4 = __dadd_rn(s4, __dmul_rn(t2, (double)(am * am)));
+                const unsigned long long am = (unsigned long long)(m < 0 ? -m : m);  // <= N <= 16384
+                const unsigned long long am2 = am * am;
+                a0 += H;
+                a1 += (u128)H * am;
+                a2 += (u128)H * am2;
+                a4 += (u128)H * (am2 * am2);
             }
+#pragma unroll
+            for (int k = 0; k < kObsUnroll; ++k) h[k] = hn[k];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a0 += shfl_xor_u128(a0, o);
+            a1 += shfl_xor_u128(a1, o);
+            a2 += shfl_xor_u128(a2, o);
+            a4 += shfl_xor_u128(a4, o);
+        }
+        if (ln == 0 && a0 != 0) {
+            const double bz = exp(__dsub_rn(__dmul_rn(nbd, (double)i), lnw[i]));
+            s0 = __dadd_rn(s0, __dmul_rn(u128_to_double(a0), bz));
+            s1 = __dadd_rn(s1, __dmul_rn(u128_to_double(a1), bz));
+            s2 = __dadd_rn(s2, __dmul_rn(u128_to_double(a2), bz));
+            s4 = __dadd_rn(s4, __dmul_rn(u128_to_double(a4), bz));
         }
     }
     __shared__ double sh[4][kObsThreads / 32];
