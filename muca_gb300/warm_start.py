@@ -59,25 +59,110 @@ def train(net, x, t, schedule=((10000, 1e-3), (10000, 3e-4), (10000, 1e-4)), bat
                            for k, (steps, lr) in enumerate(schedule)])
 
 
-def ab_test(net, held, opts=RUN_OPTS, device=0):
-    """Zero weight against the network's weight on the same held-out
-    instances (same seeds, same options)."""
-    warm = [net.log_weights(L, T, D) for L, _, T, D, _ in held]
+# Knots of the reference's piecewise-linear extrapolation, as fractions of N:
+# E_Delta = 0, 0.176 N, 0.888 N and N (muca_delta_multigpu.cu:271-307, code
+# commented out there).  Between the knots the reference adds straight lines
+# whose heights it fitted by hand for one (L, T).
+PL_KNOTS = (0.0, 0.176, 0.888, 1.0)
+
+
+def _bracket(keys, x):
+    """Indices (a, b) of the two entries of the sorted `keys` that bracket x,
+    or the two nearest ones when x lies outside; lam = (x - ka) / (kb - ka)."""
+    b = int(np.clip(np.searchsorted(keys, x), 1, len(keys) - 1))
+    ka, kb = keys[b - 1], keys[b]
+    return b - 1, b, ((x - ka) / (kb - ka) if kb != ka else 0.0)
+
+
+def _at_size(L, T, sources, knots):
+    same = sorted(((float(Ts), np.asarray(w, np.float64)) for Ls, Ts, w in sources if Ls == L),
+                  key=lambda s: s[0])
+    N = L * L
+    i = np.arange(N + 1, dtype=np.float64)
+
+    def shape(w):
+        if w.size != N + 1:
+            raise ValueError(f"weight of L={L} has {w.size} entries, not {N + 1}")
+        if knots is None:
+            return w
+        ik = np.unique(np.rint(np.asarray(knots, np.float64) * N).astype(np.int64))
+        return np.interp(i, ik, w[ik])
+
+    if len(same) == 1:
+        out = shape(same[0][1])
+    else:
+        a, b, lam = _bracket(np.array([s[0] for s in same]), T)
+        out = (1.0 - lam) * shape(same[a][1]) + lam * shape(same[b][1])
+    return out - out.mean()
+
+
+def interpolated_weight(L, T, sources, knots=None):
+    """A non-learned initial lnW for (L, T) from converged weights
+    sources [(L, T, lnW)].  Per lattice size, the two sources nearest in
+    temperature (bracketing T where they can) are interpolated linearly in T
+    (extrapolated outside).  With `knots` (fractions of N) each source is
+    first reduced to the straight lines through its values at those E_Delta:
+    the form of the reference's extrapolation, with the knot heights taken
+    from data instead of fitted by hand.  For a size with no source, the two
+    nearest sizes are combined the same way, linearly in L, as lnW/N on the
+    common axis E_Delta/N (lnW is extensive).  Returns lnW of mean zero (a
+    constant shift leaves the iteration unchanged)."""
+    sizes = sorted({int(Ls) for Ls, _, _ in sources})
+    if not sizes:
+        raise ValueError("no converged weight to interpolate from")
+    if L in sizes:
+        return _at_size(L, T, sources, knots)
+    N = L * L
+    x = np.arange(N + 1, dtype=np.float64) / N
+
+    def per_site(Ls):
+        w = _at_size(Ls, T, sources, knots)
+        Ns = Ls * Ls
+        return np.interp(x, np.arange(Ns + 1, dtype=np.float64) / Ns, w / Ns)
+
+    if len(sizes) == 1:
+        out = N * per_site(sizes[0])
+    else:
+        a, b, lam = _bracket(np.array(sizes, np.float64), float(L))
+        out = N * ((1.0 - lam) * per_site(sizes[a]) + lam * per_site(sizes[b]))
+    return out - out.mean()
+
+
+def ab_test(net, held, opts=RUN_OPTS, device=0, sources=None):
+    """The zero weight against the network's weight on the same held-out
+    instances (same seeds, same options).  With `sources` ([(L, T, lnW)],
+    the converged training weights) two non-learned arms run beside them:
+    "pl", the reference's piecewise-linear form (knots PL_KNOTS) with knot
+    heights interpolated in T, and "interp", the full converged weights
+    interpolated in T."""
+    arms = {"mlp": [net.log_weights(L, T, D) for L, _, T, D, _ in held]}
+    if sources is not None:
+        arms["pl"] = [interpolated_weight(L, T, sources, PL_KNOTS) for L, _, T, _, _ in held]
+        arms["interp"] = [interpolated_weight(L, T, sources) for L, _, T, _, _ in held]
     rz, sz, wz = converge(held, opts, None, device)
-    rm, sm, _ = converge(held, opts, warm, device)
+    runs = {k: converge(held, opts, w, device)[:2] for k, w in arms.items()}
     rows = []
     for i, (L, nc, T, D, seed) in enumerate(held):
-        e = warm[i] - wz[i]
-        rows.append({"L": L, "T": T, "delta": D, "chains": nc, "zero_iters": rz[i].iterations,
-                     "zero_converged": bool(rz[i].converged), "mlp_iters": rm[i].iterations,
-                     "mlp_converged": bool(rm[i].converged),
-                     "surrogate_lnw_rms_err": float(np.sqrt(np.mean((e - e.mean()) ** 2))),
-                     "lnw_range": float(wz[i].max() - wz[i].min())})
+        row = {"L": L, "T": T, "delta": D, "chains": nc, "zero_iters": rz[i].iterations,
+               "zero_converged": bool(rz[i].converged), "lnw_range": float(wz[i].max() - wz[i].min())}
+        for k, (r, _) in runs.items():
+            e = arms[k][i] - wz[i]
+            row[k + "_iters"] = r[i].iterations
+            row[k + "_converged"] = bool(r[i].converged)
+            row[k + "_lnw_rms_err"] = float(np.sqrt(np.mean((e - e.mean()) ** 2)))
+        row["surrogate_lnw_rms_err"] = row["mlp_lnw_rms_err"]
+        rows.append(row)
     iz = sum(r["zero_iters"] for r in rows)
-    im = sum(r["mlp_iters"] for r in rows)
-    return {"instances": rows, "zero_iters_total": iz, "mlp_iters_total": im,
-            "iters_ratio": iz / max(1, im), "zero_device_s": sz, "mlp_device_s": sm,
-            "time_ratio": sz / sm if sm > 0 else None}
+    out = {"instances": rows, "zero_iters_total": iz, "zero_device_s": sz}
+    for k, (_, s) in runs.items():
+        ik = sum(r[k + "_iters"] for r in rows)
+        out[k + "_iters_total"] = ik
+        out[k + "_device_s"] = s
+        out[k + "_iters_ratio"] = iz / max(1, ik)
+        out[k + "_time_ratio"] = sz / s if s > 0 else None
+    out["iters_ratio"] = out["mlp_iters_ratio"]
+    out["time_ratio"] = out["mlp_time_ratio"]
+    return out
 
 
 def main(argv=None):
@@ -86,11 +171,13 @@ def main(argv=None):
     p.add_argument("--chains", type=int, default=1024)
     p.add_argument("--t-step", type=float, default=0.025)
     p.add_argument("--held-T", default="0.53,0.67")
+    p.add_argument("--held-L", default="", help="held-out lattice sizes beyond the training ones")
     p.add_argument("--steps", type=int, default=10000, help="Adam steps per learning-rate stage (3 stages)")
     p.add_argument("--schedule", type=int, default=RUN_OPTS["nup_schedule"])
     p.add_argument("--device", type=int, default=0)
     a = p.parse_args(argv)
     Ls = [int(v) for v in a.L.split(",")]
+    held_L = [int(v) for v in a.held_L.split(",") if v]
     Ts = np.round(np.arange(0.40, 0.8 + 1e-9, a.t_step), 4)
     rng = np.random.default_rng(0)
     opts = dict(RUN_OPTS, nup_schedule=a.schedule)
@@ -110,8 +197,9 @@ def main(argv=None):
                "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
                "wall_s": time.time() - t0}
         held = [(L, a.chains, float(T), float(rng.uniform(1.5, 1.99)), 5000 + k)
-                for k, (L, T) in enumerate([(L, float(T)) for L in Ls for T in a.held_T.split(",")])]
-        ab = ab_test(net, held, opts, a.device)
+                for k, (L, T) in enumerate([(L, float(T)) for L in Ls + held_L for T in a.held_T.split(",")])]
+        sources = [(train_inst[i][0], train_inst[i][2], W[i]) for i in ok]
+        ab = ab_test(net, held, opts, a.device, sources)
     out = {"run_opts": {k: v for k, v in opts.items()}, "training_set": gen, "fit": fit, "ab": ab}
     print(json.dumps(out))
     return out

@@ -2,7 +2,8 @@
 the batched engine train the MLP on the device; on held-out (L, T) the weight
 iteration from the network's prediction reaches the same flat-histogram
 criterion in far fewer iterations than from the zero weight (same seeds,
-same options)."""
+same options).  The two non-learned arms (the reference's piecewise-linear
+form and the full weights, interpolated in T) run beside it and converge."""
 import numpy as np
 import pytest
 
@@ -21,9 +22,10 @@ def test_warm_start_cuts_iterations(muca):
     with muca.MLP(seed=7) as net:
         losses = ws.train(net, x, t, schedule=((3000, 1e-3), (3000, 3e-4)))
         assert losses[-100:].mean() < 1e-3 * losses[:10].mean()
-        ab = ws.ab_test(net, held)
+        sources = [(L, T, w) for (L, _, T, _, _), w in zip(train_inst, W)]
+        ab = ws.ab_test(net, held, sources=sources)
     rows = ab["instances"]
-    assert all(r["zero_converged"] and r["mlp_converged"] for r in rows)
+    assert all(r[k + "_converged"] for r in rows for k in ("zero", "mlp", "pl", "interp"))
     assert ab["iters_ratio"] >= 2.0, ab
     # the surrogate is within a few units of lnW over a range of hundreds
     for r in rows:
