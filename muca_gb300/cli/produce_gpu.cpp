@@ -20,6 +20,14 @@
 //                  reference's error column is NaN, with blocks it is not;
 //   --binder       also writes the Binder cumulant U4 = 1 - <M^4>/(3<M^2>^2)
 //                  per Delta point to observables_binder_gpu...;
+//   --reuse-histogram  one thermalisation and one production run (with the
+//                  first Delta point's seeds) serve every Delta point.  The
+//                  sweep's weights are the file's at every point (the shift
+//                  only enters the reweighting), so the simulation does not
+//                  depend on Delta and each point only reweights the same
+//                  histogram(s) with its own shifted weights: `range` times
+//                  fewer sweeps.  The first line equals the one without the
+//                  option;
 //   ./fss/L<L> is created when missing.
 #include <fstream>
 #include <iomanip>
@@ -36,7 +44,8 @@ int main(int argc, char **argv)
     if (pos.size() < 9) {
         std::fprintf(stderr,
                      "usage: %s L first_gpu last_gpu range jacks therm_mult nup_mult delta gap\n"
-                     "          [--device=D] [--chains=NW] [--jack-blocks] [--binder] [--kernel=0..3]\n",
+                     "          [--device=D] [--chains=NW] [--jack-blocks] [--binder] [--reuse-histogram]\n"
+                     "          [--kernel=0..3]\n",
                      argv[0]);
         return 2;
     }
@@ -53,6 +62,7 @@ int main(int argc, char **argv)
         return 2;
     }
     const bool blocks = opt.has("jack-blocks") && JACKS > 0;
+    const bool reuse = opt.has("reuse-histogram");
     const int device = (int)opt.num("device", first_gpu);
     uint32_t NUM_WORKERS = 0;
     if (opt.has("chains")) {
@@ -105,7 +115,59 @@ int main(int argc, char **argv)
     std::vector<double> avg_M(range), error_M(range), avg_sus(range), error_sus(range), avg_u4(range),
         error_u4(range);
     const unsigned nj = blocks ? JACKS : NofGPU;
-    for (unsigned l = 0; l < range; l++) {
+    if (reuse) {
+        // [l][unit]: the jackknife quantities of every Delta point
+        std::vector<double> Mq((size_t)range * nj), Sq((size_t)range * nj), Uq((size_t)range * nj);
+        std::vector<double> sums((size_t)range * nj * 4, 0.0);
+        // reweights the device's current histogram at every Delta point, with
+        // the reweighting weights shifted from the file's exactly as the loop
+        // below shifts them point by point
+        auto scan_deltas = [&](unsigned unit, unsigned g) {
+            if (muca_set_weights(ctx[g], log_weight.data(), N + 1) != MUCA_OK) cli::die("set weights", ctx[g]);
+            double d = delta_i;
+            for (unsigned l = 0; l < range; ++l) {
+                d = d + gap / (double)range;
+                if (muca_weight_shift(ctx[g], beta, d) != MUCA_OK) cli::die("weight shift", ctx[g]);
+                muca_observables o{};
+                if (muca_compute_observables(ctx[g], beta, d, &o) != MUCA_OK) cli::die("observables", ctx[g]);
+                const size_t k = (size_t)l * nj + unit;
+                Mq[k] = o.m_abs;
+                Sq[k] = o.chi;
+                Uq[k] = o.u4;
+                sums[4 * k] += o.sum;
+                sums[4 * k + 1] += o.m1;
+                sums[4 * k + 2] += o.m2;
+                sums[4 * k + 3] += o.m4;
+            }
+        };
+        // the first Delta point's thermalisation and production seeds (l = 0)
+        for (unsigned g = 0; g < NofGPU; ++g)
+            if (muca_sweep(ctx[g], 0, 100u, 1000u, therm_run, 0) != MUCA_OK) cli::die("sweep", ctx[g]);
+        if (!blocks) {
+            for (unsigned g = 0; g < NofGPU; ++g)
+                if (muca_sweep(ctx[g], 0, 100u, 2000u, 0, NUPDATES) != MUCA_OK) cli::die("sweep", ctx[g]);
+            for (unsigned g = 0; g < NofGPU; ++g) scan_deltas(g, g);
+        } else {
+            for (unsigned jj = 0; jj < JACKS; ++jj)
+                for (unsigned g = 0; g < NofGPU; ++g) {
+                    if (muca_sweep(ctx[g], jj, 100u, 2000u, 0, NUPDATES) != MUCA_OK) cli::die("sweep", ctx[g]);
+                    scan_deltas(jj, g);
+                }
+            for (size_t k = 0; k < (size_t)range * nj; ++k) {
+                const double s = sums[4 * k], m1 = sums[4 * k + 1], m2 = sums[4 * k + 2], m4 = sums[4 * k + 3];
+                Mq[k] = m1 / s;
+                Sq[k] = (m2 / s - (m1 / s) * (m1 / s)) * beta / (double)N;
+                Uq[k] = 1.0 - (m4 / s) / (3.0 * (m2 / s) * (m2 / s));
+            }
+        }
+        for (unsigned l = 0; l < range; l++) {
+            const size_t k = (size_t)l * nj;
+            muca_jackknife(ctx[0], &Mq[k], nj, &avg_M[l], &error_M[l]);
+            muca_jackknife(ctx[0], &Sq[k], nj, &avg_sus[l], &error_sus[l]);
+            muca_jackknife(ctx[0], &Uq[k], nj, &avg_u4[l], &error_u4[l]);
+        }
+    }
+    for (unsigned l = 0; l < range && !reuse; l++) {
         std::cout << "L" << Ls << " Progress...  " << 100 * l / range << "%" << "\r" << std::flush;
         delta = delta + gap / (double)range;
         for (unsigned g = 0; g < NofGPU; ++g) {

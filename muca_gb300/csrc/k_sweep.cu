@@ -29,10 +29,10 @@
 //     lane, so every decision equals the reference's logf decision.
 // Kernels:
 //   k_sweep_spec  warp-specialised: per 32 chains one producer warp draws the
-//                 Philox numbers (two blocks per four attempts) into a
-//                 4-deep shared-memory ring guarded by mbarriers, and one
-//                 consumer warp runs decode, scan, write-back and histogram;
-//                 the producer's integer work fills the consumer's latency;
+//                 Philox numbers and decodes each window into a 2-deep
+//                 shared-memory ring guarded by mbarriers, and one consumer
+//                 warp runs the scan, write-back and histogram; two
+//                 independent instruction streams per 32 chains;
 //   k_sweep_win   the same window core with the Philox numbers drawn by the
 //                 chain's own lane, one window ahead;
 //   k_sweep_generic  the reference step by step on the packed layout, any L.
@@ -89,6 +89,79 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long l
 
 constexpr long long kWaitCycles = 1ll << 34;  // ~8 s at 2 GHz; a normal launch takes milliseconds
 
+// Slot words (index f: shared u32 at slot[32 f], one column per lane).
+enum SlotWord : uint32_t {
+    kSlotC = 0,     // the window's lattice word as the producer read it
+    kSlotV = 1,     // proposed codes (nibbles)
+    kSlotDD = 2,    // dDelta + 1 (nibbles)
+    kSlotDV = 3,    // s_new - s_old + 2 (nibbles; production only)
+    kSlotDE = 4,    // dE as signed bytes, sites 0..3 and 4..7 (two words)
+    kSlotF2 = 6,    // -beta dE as floats (8 words)
+    kSlotLF = 14,   // __logf(u) (8 words)
+    kSlotP = 22,    // packed draws (8 words): the exact replay and partial windows
+};
+static_assert(kSlotP + 8 == kSlotWords, "slot layout");
+
+// The producer's half of a window: decode (as decode_window) and store the
+// fields the consumer's scan needs into the slot.
+template <int MODE, int SLOTS>
+__device__ __forceinline__ void put_window(const WinDec<MODE> &d, uint32_t *slot)
+{
+    slot[32 * kSlotC] = d.C;
+    slot[32 * kSlotV] = d.vnib;
+    uint32_t dd = 0, dv = 0, e0 = 0, e1 = 0;
+#pragma unroll
+    for (int t = 0; t < SLOTS; ++t) {
+        dd |= (uint32_t)(d.dDel[t] + 1) << (4 * t);
+        dv |= (uint32_t)(d.dM[t] + 2) << (4 * t);
+        if (t < 4) e0 |= ((uint32_t)d.dE[t] & 0xFFu) << (8 * t);
+        else       e1 |= ((uint32_t)d.dE[t] & 0xFFu) << (8 * (t - 4));
+        slot[32 * (kSlotF2 + t)] = __float_as_uint(d.f2[t]);
+        slot[32 * (kSlotLF + t)] = __float_as_uint(d.lf[t]);
+        slot[32 * (kSlotP + t)] = d.p[t];
+    }
+    slot[32 * kSlotDD] = dd;
+    if (MODE == kModeProduce) slot[32 * kSlotDV] = dv;
+    slot[32 * kSlotDE] = e0;
+    if (SLOTS > 4) slot[32 * (kSlotDE + 1)] = e1;
+}
+
+// The consumer's half: the decoded window back from the slot.  The word the
+// producer read is still the word in the lattice: this parity's bits of it
+// change only at this window, the other parity's only in the other half.
+template <int MODE, int SLOTS>
+__device__ __forceinline__ void get_window(const uint32_t *slot, uint32_t *pc, uint32_t half, WinDec<MODE> &d)
+{
+    constexpr uint32_t M2 = 0x33333333u;
+    d.pc = pc;
+    d.C = slot[32 * kSlotC];
+    d.hs0 = half ? 2u : 0u;
+    d.ctr = (d.C >> d.hs0) & M2;
+    d.vnib = slot[32 * kSlotV];
+    const uint32_t dd = slot[32 * kSlotDD];
+    const uint32_t dv = MODE == kModeProduce ? slot[32 * kSlotDV] : 0u;
+    const uint32_t e0 = slot[32 * kSlotDE];
+    const uint32_t e1 = SLOTS > 4 ? slot[32 * (kSlotDE + 1)] : 0u;
+#pragma unroll
+    for (int t = 0; t < SLOTS; ++t) {
+        d.dDel[t] = (int)((dd >> (4 * t)) & 3u) - 1;
+        d.dM[t] = MODE == kModeProduce ? (int)((dv >> (4 * t)) & 7u) - 2 : 0;
+        d.dE[t] = (int)(signed char)(uint8_t)((t < 4 ? e0 : e1) >> (8 * (t & 3)));
+        d.f2[t] = __uint_as_float(slot[32 * (kSlotF2 + t)]);
+        d.lf[t] = __uint_as_float(slot[32 * (kSlotLF + t)]);
+    }
+    d.pr = slot + 32 * kSlotP;
+}
+
+// Per 32 chains one producer warp and one consumer warp.  The producer draws
+// the Philox numbers and decodes each window (proposals, dE, dDelta,
+// __logf(u)) into a ring slot; the consumer runs the scan, the lattice
+// store and the histogram.  Decoding window (row, q) reads the same-parity
+// word of row - 1, written by the consumer WPR windows earlier, so the ring
+// is at most WPR deep; at the start of a half (and of a phase) the producer
+// waits until every earlier window is written back, since the new half reads
+// the other parity.  A slot is released after its window's store, so a
+// released slot also means a written word.  Every wait is bounded.
 template <int MODE, int R, bool LAT_SMEM>
 __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32_t cpb)
 {
@@ -104,10 +177,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
     const uint32_t lane = pair * 32u + l32;  // chain slot in the block
     const size_t ring_off = smem_weights_bytes(MODE, a.N) + smem_hist_bytes(MODE, a.N);
     uint32_t *ring = reinterpret_cast<uint32_t *>(smem + ring_off);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + ring_off + (size_t)P * kRingDepth * 8 * 32 * 4);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + ring_off + (size_t)P * kRingDepth * kSlotWords * 32 * 4);
     uint64_t *full = bars + (size_t)pair * kRingDepth * 2;
     uint64_t *empty = full + kRingDepth;
-    uint32_t *myring = ring + (size_t)pair * kRingDepth * 8 * 32 + l32;
+    uint32_t *myring = ring + (size_t)pair * kRingDepth * kSlotWords * 32 + l32;
     if (threadIdx.x == 0) {
         for (uint32_t i = 0; i < P * kRingDepth * 2; ++i) mbar_init(bars + i, 32);
     }
@@ -118,28 +191,57 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
     float tol = 0.0f;
     uint32_t *lat = prologue<MODE, LAT_SMEM, true, DT>(a, smem, lat_off, cpb, producer ? 0xFFFFFFFFu : lane,
                                                        blockIdx.x, wS, histS, gl, &tol);
+    if (producer) {  // the pair's lattice columns (padding lanes read lane 0's)
+        const uint32_t l = lane < cpb ? lane : 0u;
+        lat = LAT_SMEM ? reinterpret_cast<uint32_t *>(smem + lat_off) + l
+                       : a.lat + (size_t)blockIdx.x * a.L * a.WPR * cpb + l;
+    }
     const double *wG = reinterpret_cast<const double *>(a.w);
     const WT *wP = DT ? reinterpret_cast<const WT *>(a.w) : wS;
     __syncthreads();
     ChainSetup<MODE, R> cs;
     cs.init(a, cpb, lane, blockIdx.x);
     const uint32_t L = a.L, WPR = a.WPR;
+    // depth 1 or 2 (a power of two): never more than WPR
+    const uint32_t dsh = WPR >= kRingDepth ? 1u : 0u;
+    const uint32_t D = 1u << dsh;
     const long long deadline = clock64() + kWaitCycles;
     uint32_t w = 0;  // window counter (ring position)
     bool ok = true;
 
     if (producer) {
         uint32_t cc = 0;  // Philox counter word 0 of the last drawn group
-        for_each_window(L, WPR, a.therm, nup, [&](uint32_t, uint32_t, uint32_t, uint32_t, uint32_t len, bool) {
-            const uint32_t s = w % kRingDepth, round = w / kRingDepth;
+        for_each_window(L, WPR, a.therm, nup, [&](uint32_t row, uint32_t q, uint32_t half, uint32_t cnt,
+                                                  uint32_t len, bool) {
             uint32_t p[8];
             draw_group<R>(cc + 1, cs.seed, iter, cs.k1, cs.k3, p);
             if (len > 4) draw_group<R>(cc + 2, cs.seed, iter, cs.k1, cs.k3, p + 4);
-            cc += (len + 3u) >> 2;
-            if (!mbar_wait(empty + s, (round & 1u) ^ 1u, deadline)) { ok = false; return false; }
-            uint32_t *slot = myring + (size_t)s * 8 * 32;
 #pragma unroll
-            for (int t = 0; t < 8; ++t) slot[t * 32] = p[t];
+            for (int t = 0; t < 4; ++t)
+                if (len <= 4) p[4 + t] = 0u;
+            cc += (len + 3u) >> 2;
+            if (row == 0 && q == 0) {
+                // a new half or phase: the windows still in the ring must be written back
+                for (uint32_t j = 1; j < D && j <= w; ++j) {
+                    const uint32_t v = w - j;
+                    if (!mbar_wait(empty + (v & (D - 1u)), (v >> dsh) & 1u, deadline)) { ok = false; return false; }
+                }
+            }
+            const uint32_t s = w & (D - 1u), round = w >> dsh;
+            if (!mbar_wait(empty + s, (round & 1u) ^ 1u, deadline)) { ok = false; return false; }
+            uint32_t *slot = myring + (size_t)s * kSlotWords * 32;
+            if (len < cnt) {
+#pragma unroll
+                for (int t = 0; t < 8; ++t) slot[32 * (kSlotP + t)] = p[t];
+            } else if (cnt == 8) {
+                WinDec<MODE> d;
+                decode_window<MODE, 8>(lat, cpb, L, WPR, row, q, half, p, nullptr, d);
+                put_window<MODE, 8>(d, slot);
+            } else {
+                WinDec<MODE> d;
+                decode_window<MODE, 4>(lat, cpb, L, WPR, row, q, half, p, nullptr, d);
+                put_window<MODE, 4>(d, slot);
+            }
             mbar_arrive(full + s);
             ++w;
             return true;
@@ -154,31 +256,26 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
         const bool checked = (unsigned long long)cpb * nup >= 0xFFFFFFFFull;
         for_each_window(L, WPR, a.therm, nup, [&](uint32_t row, uint32_t q, uint32_t half, uint32_t cnt,
                                                   uint32_t len, bool rec_phase) {
-            const uint32_t s = w % kRingDepth, round = w / kRingDepth;
+            const uint32_t s = w & (D - 1u), round = w >> dsh;
             if (!mbar_wait(full + s, round & 1u, deadline)) { ok = false; return false; }
-            const uint32_t *slot = myring + (size_t)s * 8 * 32;
+            const uint32_t *slot = myring + (size_t)s * kSlotWords * 32;
             const bool rec = rec_phase && cs.active;
+            uint32_t *pc = lat + (size_t)(row * WPR + q) * cpb;
             if (len < cnt) {
                 uint32_t p[8];
 #pragma unroll
-                for (int t = 0; t < 8; ++t) p[t] = slot[t * 32];
-                mbar_arrive(empty + s);
+                for (int t = 0; t < 8; ++t) p[t] = slot[32 * (kSlotP + t)];
                 partial_core<MODE>(lat, cpb, L, WPR, row, q, half, len, rec, store, wP, histS, a.hist, st, p);
             } else if (cnt == 8) {
-                uint32_t p[8];
-#pragma unroll
-                for (int t = 0; t < 8; ++t) p[t] = slot[t * 32];
-                mbar_arrive(empty + s);
-                if (half) window_core<MODE, 8, 1>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, nullptr, 0, wG, tol);
-                else      window_core<MODE, 8, 0>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, nullptr, 0, wG, tol);
+                WinDec<MODE> d;
+                get_window<MODE, 8>(slot, pc, half, d);
+                scan_window<MODE, 8, true>(d, rec, store, checked, wS, histS, a.hist, st, eps, wG, tol);
             } else {
-                uint32_t p[4];
-#pragma unroll
-                for (int t = 0; t < 4; ++t) p[t] = slot[t * 32];
-                mbar_arrive(empty + s);
-                if (half) window_core<MODE, 4, 1>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, nullptr, 0, wG, tol);
-                else      window_core<MODE, 4, 0>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p, eps, nullptr, 0, wG, tol);
+                WinDec<MODE> d;
+                get_window<MODE, 4>(slot, pc, half, d);
+                scan_window<MODE, 4, true>(d, rec, store, checked, wS, histS, a.hist, st, eps, wG, tol);
             }
+            mbar_arrive(empty + s);  // after the store: the producer may read the word
             ++w;
             return true;
         });
@@ -353,7 +450,9 @@ SweepPlan plan_sweep(int mode, int rounds, uint32_t L, uint32_t nchains, size_t 
     const uint32_t want = std::min<uint32_t>(128u, (per_sm + 31u) / 32u * 32u);
     const size_t base = smem_weights_bytes(mode, N) + smem_hist_bytes(mode, N);
     const size_t fixed = base + (p.kernel == kKernelSpecialized ? smem_ring_bytes((want + 31u) / 32u) : 0);
-    const size_t cap = smem_optin > fixed ? (smem_optin - fixed) / per_chain : 0;
+    // keep 512 B of the opt-in limit for the kernels' static shared memory
+    const size_t optin = smem_optin > 512 ? smem_optin - 512 : 0;
+    const size_t cap = optin > fixed ? (optin - fixed) / per_chain : 0;
     uint32_t cpb = want;
     // Lattice in shared memory when a block of at least one warp fits and that
     // takes no more waves of blocks than keeping it in global memory (one

@@ -50,7 +50,10 @@ struct SweepPlan {
     uint32_t blocks;
     size_t smem;     // dynamic shared memory bytes
 };
-constexpr uint32_t kRingDepth = 4;  // windows the producer warps may run ahead
+// Warp-specialised sweep: ring slots per warp pair (the producer runs at most
+// this many decoded windows ahead), and u32 words per slot and lane.
+constexpr uint32_t kRingDepth = 2;
+constexpr uint32_t kSlotWords = 30;
 
 // Chooses placement and block shape for (mode, L, nchains) on a device with
 // `smem_optin` bytes of opt-in shared memory per block and `sms` SMs.

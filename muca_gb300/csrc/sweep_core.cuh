@@ -25,10 +25,11 @@ __host__ __device__ inline size_t smem_hist_bytes(int mode, uint32_t N)
 {
     return mode == kModeWeight ? align16((size_t)(N + 1) * 4) : 0;
 }
-// ring: [pair][depth][slot 0..7][lane 0..31] u32, then full/empty mbarriers
+// ring: [pair][depth][word 0..kSlotWords-1][lane 0..31] u32, then the
+// full/empty mbarriers of every pair and slot
 __host__ __device__ inline size_t smem_ring_bytes(uint32_t pairs)
 {
-    return (size_t)pairs * kRingDepth * 8 * 32 * 4 + (size_t)pairs * kRingDepth * 2 * 8;
+    return (size_t)pairs * kRingDepth * kSlotWords * 32 * 4 + (size_t)pairs * kRingDepth * 2 * 8;
 }
 
 struct ChainState {
@@ -138,6 +139,7 @@ struct WinDec {
     float f2[8];                // -beta dE (an even integer for beta = 2: exact in FP32 and FP64)
     float lf[8];                // __logf(u)
     uint32_t p[8];              // the packed draws (for the exact replay)
+    const uint32_t *pr;         // or, when set, the draws in shared memory (pr[32 t])
 };
 
 // Decodes the SLOTS same-parity sites (half 0: even, 1: odd) of word q of
@@ -190,6 +192,7 @@ __device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32
     const uint32_t nzn = ((vnib ^ N1) | ((vnib ^ N1) >> 1)) & N1;  // s_new != 0
     const uint32_t ddb = nzn + N1 - nzo;                           // dDel + 1 (0..2)
     const uint32_t dvb = vnib + 0x22222222u - ctr;                 // s_new - s_old + 2 (0..4)
+    d.pr = nullptr;
     d.C = C;
     d.ctr = ctr;
     d.vnib = vnib;
@@ -269,7 +272,7 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
             for (int t = 0; t < SLOTS; ++t) {
                 const double diff = __dsub_rn(__dadd_rn((double)d.f2[t], wG[st.E + d.dDel[t]]), wG[st.E]);
                 bool acc = diff >= 0.0;
-                if (!acc) acc = (double)logf(u01f(d.p[t])) < diff;
+                if (!acc) acc = (double)logf(u01f(d.pr ? d.pr[32 * t] : d.p[t])) < diff;
                 acc = acc && store;
                 if (acc) {
                     st.E += d.dDel[t];
@@ -346,7 +349,7 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
             else
                 diff = __dsub_rn(__dadd_rn((double)d.f2[t], (double)wn), (double)wE);
             bool acc = diff >= (WT)0;
-            if (!acc) acc = (WT)logf(u01f(d.p[t])) < diff;
+            if (!acc) acc = (WT)logf(u01f(d.pr ? d.pr[32 * t] : d.p[t])) < diff;
             acc = acc && store;
             if (acc) {
                 st.E += d.dDel[t];

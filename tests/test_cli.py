@@ -90,33 +90,57 @@ def test_multigpu_weight_matches_oracle(exes, orc, tmp_path):
 
 def _produce_restated(orc, L, NW, ndev, rng_, tm, nm, delta0, gap, lnw_file):
     """produce2_multigpu.cu main (:91-363) restated with oracle routines."""
-    Lb = orc.lib()
+    return [(m, s) for m, s, _ in _produce_variants(orc, L, NW, ndev, rng_, 0, tm, nm, delta0, gap, lnw_file)]
+
+
+def _produce_variants(orc, L, NW, ndev, rng_, jacks, tm, nm, delta0, gap, lnw_file, blocks=False, reuse=False):
+    """The production loop with the options of produce_gpu: `blocks`
+    jackknifes over `jacks` production blocks (seeds of the block loop at
+    produce2_multigpu.cu:324-347, iter jj, seed 100 + l + 2000 g), `reuse`
+    runs the thermalisation and production of the first Delta point only and
+    reweights its histograms at every point.  Returns per Delta point the
+    jackknifed (<|M|>, chi, U4) as (avg, err) pairs."""
     N = L * L
     beta = 2.0
-    lnw_host = lnw_file.copy()
     lats, ejs, eds, mgs = [], [], [], []
     for g in range(ndev):
         lat = orc.init_lattice(L, NW, orc.scheme_produce(g)).copy()
         ej, ed, mg = orc.energies(L, lat)
         lats.append(lat); ejs.append(ej); eds.append(ed); mgs.append(mg)
-    out = []
-    delta = delta0
+    deltas, d = [], delta0
     for l in range(rng_):
-        delta = delta + gap / rng_
-        Lb.orc_weight_shift(beta, delta, N, lnw_host)
+        d = d + gap / rng_
+        deltas.append(d)
+    boltz = []
+    lnw_host = lnw_file.copy()
+    for d in deltas:
+        orc.lib().orc_weight_shift(beta, d, N, lnw_host)
         bz = np.zeros(N + 1)
-        Lb.orc_boltz(beta, delta, N, lnw_host, bz, 0)
-        mj, sj = [], []
+        orc.lib().orc_boltz(beta, d, N, lnw_host, bz, 0)
+        boltz.append(bz)
+    nu = jacks if blocks else ndev
+    q = np.zeros((rng_, nu, 3))
+    sums = np.zeros((rng_, nu, 4))
+    for l in range(1 if reuse else rng_):
         for g in range(ndev):
             lats[g], _ = orc.produce_sweep(L, lats[g], ejs[g], eds[g], mgs[g], lnw_file, 0, 100 + 1000 * g + l,
                                            N * tm, 0, nthreads=8)
-        for g in range(ndev):
-            lats[g], h = orc.produce_sweep(L, lats[g], ejs[g], eds[g], mgs[g], lnw_file, l, 100 + 2000 * g, 0,
-                                           N * nm, nthreads=8)
-            o = orc.observables(beta, N, h, bz)
-            mj.append(o[0]); sj.append(o[1])
-        out.append((orc.jackknife(np.array(mj)), orc.jackknife(np.array(sj))))
-    return out
+        pts = range(rng_) if reuse else [l]
+        for u in range(nu):
+            for g in (range(ndev) if blocks else [u]):
+                it, seed = (u, 100 + l + 2000 * g) if blocks else (l, 100 + 2000 * g)
+                lats[g], h = orc.produce_sweep(L, lats[g], ejs[g], eds[g], mgs[g], lnw_file, it, seed, 0, N * nm,
+                                               nthreads=8)
+                for k in pts:
+                    o = orc.observables(beta, N, h, boltz[k])
+                    q[k, u] = o[:3]
+                    sums[k, u] += o[3:]
+    if blocks:
+        s, m1, m2, m4 = (sums[..., i] for i in range(4))
+        q[..., 0] = m1 / s
+        q[..., 1] = (m2 / s - (m1 / s) ** 2) * beta / N
+        q[..., 2] = 1.0 - (m4 / s) / (3.0 * (m2 / s) ** 2)
+    return [tuple(orc.jackknife(q[k, :, i]) for i in range(3)) for k in range(rng_)]
 
 
 @pytest.mark.gpu
@@ -145,3 +169,61 @@ def test_produce_gpu_matches_oracle(exes, orc, tmp_path):
         # later lines with the 10 digits set by the first line's setprecision
         np.testing.assert_allclose(row[0], 1.9 + 0.1 * (i + 1) / rng_, rtol=1e-5 if i == 0 else 1e-9)
         np.testing.assert_allclose(row[1:], [m[0], m[1], s[0], s[1]], rtol=2e-9, atol=1e-12)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("opts", [["--jack-blocks", "--binder"], ["--reuse-histogram", "--binder"],
+                                  ["--reuse-histogram", "--jack-blocks"]])
+def test_produce_gpu_options_match_oracle(exes, orc, tmp_path, opts):
+    L, NW, ndev, rng_, jacks, tm, nm = 4, 128, 2, 3, 3, 10, 30
+    N = L * L
+    d = tmp_path / "fss" / ("L%d" % L)
+    d.mkdir(parents=True)
+    rng = np.random.default_rng(11)
+    lnw = np.cumsum(rng.normal(-0.8, 0.4, N + 1))
+    lnw -= lnw[0]
+    with open(d / "weight_mpi_T050c16_M200_JACK0_DKL1e-4.txt", "w") as f:
+        for i, v in enumerate(lnw):
+            f.write("%d %.10g\n" % (i, v))
+    lnw_file = np.array([float("%.10g" % v) for v in lnw])
+    args = [str(L), "0", str(ndev - 1), str(rng_), str(jacks), str(tm), str(nm), "1.9", "0.1"]
+    r = subprocess.run([exes[1]] + args + ["--chains=%d" % NW] + opts, capture_output=True, text=True,
+                       cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stderr
+    exp = _produce_variants(orc, L, NW, ndev, rng_, jacks, tm, nm, 1.9, 0.1, lnw_file,
+                            blocks="--jack-blocks" in opts, reuse="--reuse-histogram" in opts)
+    name = "observables_gpu%d_T050_JACKgpu_THERM%sN_NUP%sN_delta1.9to0.1noreset.txt" % (ndev, tm, nm)
+    rows = [list(map(float, ln.split())) for ln in (d / name).read_text().splitlines()]
+    assert len(rows) == rng_
+    for (m, s, _), row in zip(exp, rows):
+        assert np.all(np.isfinite(row))
+        np.testing.assert_allclose(row[1:], [m[0], m[1], s[0], s[1]], rtol=2e-9, atol=1e-12)
+    if "--binder" in opts:
+        bname = "observables_binder_gpu%d_T050_THERM%sN_NUP%sN_delta1.9to0.1.txt" % (ndev, tm, nm)
+        lines = (d / bname).read_text().splitlines()
+        assert lines[0].startswith("#")
+        brows = [list(map(float, ln.split())) for ln in lines[1:]]
+        assert len(brows) == rng_
+        for (_, _, u), row in zip(exp, brows):
+            np.testing.assert_allclose(row[1:], [u[0], u[1]], rtol=2e-9, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_produce_gpu_reuse_first_point_is_the_plain_run(exes, tmp_path):
+    L, NW, ndev, rng_, tm, nm = 8, 256, 1, 4, 10, 20
+    N = L * L
+    outs = []
+    for k, extra in enumerate([[], ["--reuse-histogram"]]):
+        d = tmp_path / str(k) / "fss" / ("L%d" % L)
+        d.mkdir(parents=True)
+        with open(d / "weight_mpi_T050c16_M200_JACK0_DKL1e-4.txt", "w") as f:
+            for i in range(N + 1):
+                f.write("%d %.10g\n" % (i, -0.9 * i))
+        args = [str(L), "0", str(ndev - 1), str(rng_), "2", str(tm), str(nm), "1.5", "0.4"]
+        r = subprocess.run([exes[1]] + args + ["--chains=%d" % NW] + extra, capture_output=True, text=True,
+                           cwd=tmp_path / str(k), timeout=600)
+        assert r.returncode == 0, r.stderr
+        name = "observables_gpu%d_T050_JACKgpu_THERM%sN_NUP%sN_delta1.5to0.4noreset.txt" % (ndev, tm, nm)
+        outs.append((d / name).read_text().splitlines())
+    assert outs[0][0] == outs[1][0]
+    assert outs[0][1:] != outs[1][1:]
