@@ -55,10 +55,23 @@ __device__ __forceinline__ uint32_t pick(const uint4 &v, int i)
     return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
-// u01fixedpt<float>(r) = (1 | (r >> 8)) * 2^-24, exact in FP32.
+// u01fixedpt<float>(r) = (1 | (r >> 8)) * 2^-24 = (2k + 1) 2^-24 with
+// k = r >> 9 < 2^23, exact in FP32.  Formed without an int-to-float
+// conversion: the float with exponent 0 and mantissa k is 1 + k 2^-23, and
+// subtracting 1 - 2^-24 leaves (2k + 1) 2^-24, which has 24 significant bits
+// and is therefore the exact (and so the correctly rounded) difference.
+// Checked against the conversion form for all 2^23 values of k.
 __device__ __forceinline__ float u01f(uint32_t r)
 {
-    return __uint2float_rn((r >> 8) | 1u) * 5.9604644775390625e-08f;
+    return __fsub_rn(__uint_as_float(0x3F800000u | (r >> 9)), __uint_as_float(0x3F7FFFFFu));
+}
+
+// (float)k for a small integer k (|k| < 2^22) without an int-to-float
+// conversion: 1.5 * 2^23 + k is exact in FP32 (its ulp is 1), and so is the
+// difference with 1.5 * 2^23.
+__device__ __forceinline__ float small_int_to_float(int k)
+{
+    return __fsub_rn(__int_as_float(0x4B400000 + k), 12582912.0f);
 }
 
 // Initial spin (u < 1/3.0) + (u < 2/3.0) - 1 with the float u compared in

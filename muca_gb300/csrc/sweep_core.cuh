@@ -74,11 +74,14 @@ __device__ __forceinline__ void record(uint32_t *histS, unsigned long long *hist
     }
 }
 
-// Histogram entries of one window, merged into runs of equal bins per lane
-// (E_Delta moves by at most one per attempt, so a window's entries cluster).
-// `checked` (uniform: the launch can put 2^32 entries into one block's bins)
-// drains a u32 shared bin into the u64 device histogram once it holds 2^31.
-// HS = false (weight mode): the runs go straight to the u64 device histogram.
+// Histogram entries of one window.  Weight mode with the shared u32
+// histogram: one shared atomic per attempt; `checked` (uniform: the launch
+// can put 2^32 entries into one block's bins) drains a u32 shared bin into
+// the u64 device histogram once it holds 2^31.  Device (u64) histograms:
+// the entries are merged into runs of equal bins per lane first (E_Delta
+// moves by at most one per attempt, so a window's entries cluster), which
+// saves global atomics; HS = false (weight mode) sends the runs straight to
+// the u64 device histogram.
 template <int MODE, int SLOTS, bool HS = true>
 __device__ __forceinline__ void record_window(uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
                                               const int (&Es)[SLOTS], const int (&Ms)[SLOTS], bool checked)
@@ -103,16 +106,10 @@ __device__ __forceinline__ void record_window(uint32_t *__restrict__ histS, unsi
             }
             return;
         }
-        int cur = Es[0];
-        uint32_t cnt = 1;
+        // one fire-and-forget shared atomic per attempt: cheaper in issue
+        // slots than merging runs of equal bins first (measured)
 #pragma unroll
-        for (int t = 1; t < SLOTS; ++t) {
-            const bool same = Es[t] == cur;
-            if (!same) atomicAdd(&histS[cur], cnt);
-            cnt = same ? cnt + 1u : 1u;
-            cur = Es[t];
-        }
-        atomicAdd(&histS[cur], cnt);
+        for (int t = 0; t < SLOTS; ++t) atomicAdd(&histS[Es[t]], 1u);
     } else {
         uint32_t cur = (uint32_t)(Ms[0] + Es[0] * Es[0] + 2 * Es[0]) >> 1;
         unsigned long long cnt = 1;
@@ -204,7 +201,7 @@ __device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32
         d.dE[t] = dv * (4 - (int)((nbs >> (4 * t)) & 15u));  // -(s_new - s_old) * (sum of neighbour spins)
         d.dM[t] = dv;
         if (BT) d.f2[t] = btab[d.dE[t] + 8];
-        else    d.f2[t] = (float)(-2 * d.dE[t]);
+        else    d.f2[t] = small_int_to_float(-2 * d.dE[t]);
         d.lf[t] = __logf(u01f(p[t]));
         d.p[t] = p[t];
     }
