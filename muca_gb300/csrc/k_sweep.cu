@@ -213,12 +213,12 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
         uint32_t cc = 0;  // Philox counter word 0 of the last drawn group
         for_each_window(L, WPR, a.therm, nup, [&](uint32_t row, uint32_t q, uint32_t half, uint32_t cnt,
                                                   uint32_t len, bool) {
-            uint32_t p[8];
-            draw_group<R>(cc + 1, cs.seed, iter, cs.k1, cs.k3, p);
-            if (len > 4) draw_group<R>(cc + 2, cs.seed, iter, cs.k1, cs.k3, p + 4);
+            uint32_t r1[8], r3[8];
+            draw_pair<R>(cc + 1, cs.seed, iter, cs.k1, cs.k3, r1, r3);
+            if (len > 4) draw_pair<R>(cc + 2, cs.seed, iter, cs.k1, cs.k3, r1 + 4, r3 + 4);
 #pragma unroll
             for (int t = 0; t < 4; ++t)
-                if (len <= 4) p[4 + t] = 0u;
+                if (len <= 4) r1[4 + t] = r3[4 + t] = 0u;
             cc += (len + 3u) >> 2;
             if (row == 0 && q == 0) {
                 // a new half or phase: the windows still in the ring must be written back
@@ -232,14 +232,14 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
             uint32_t *slot = myring + (size_t)s * kSlotWords * 32;
             if (len < cnt) {
 #pragma unroll
-                for (int t = 0; t < 8; ++t) slot[32 * (kSlotP + t)] = p[t];
+                for (int t = 0; t < 8; ++t) slot[32 * (kSlotP + t)] = pack_draw(r1[t], r3[t]);
             } else if (cnt == 8) {
                 WinDec<MODE> d;
-                decode_window<MODE, 8>(lat, cpb, L, WPR, row, q, half, p, nullptr, d);
+                decode_window<MODE, 8>(lat, cpb, L, WPR, row, q, half, r1, r3, nullptr, d);
                 put_window<MODE, 8>(d, slot);
             } else {
                 WinDec<MODE> d;
-                decode_window<MODE, 4>(lat, cpb, L, WPR, row, q, half, p, nullptr, d);
+                decode_window<MODE, 4>(lat, cpb, L, WPR, row, q, half, r1, r3, nullptr, d);
                 put_window<MODE, 4>(d, slot);
             }
             mbar_arrive(full + s);

@@ -42,19 +42,20 @@ struct ChainState {
 // r3 < 2^31, so the bit is r3's top bit, set for s -> s-1).
 __device__ __forceinline__ uint32_t pack_draw(uint32_t r1, uint32_t r3) { return (r1 & 0xFFFFFF00u) | (r3 >> 31); }
 
+// One Philox block of the acceptance stream (k1) and one of the direction
+// stream (k3) at the same counter (muca_delta_multigpu.cu:794-797), kept
+// apart: r1[] the acceptance words (u01fixedpt uses their bits 31..9 only,
+// as it does those of a packed word), r3[] the direction words (bit 31).
 template <int R>
-__device__ __forceinline__ void draw_group(uint32_t cc, uint32_t seed, uint32_t iter, const RoundKeys<R> &k1,
-                                           const RoundKeys<R> &k3, uint32_t *p)
+__device__ __forceinline__ void draw_pair(uint32_t cc, uint32_t seed, uint32_t iter, const RoundKeys<R> &k1,
+                                          const RoundKeys<R> &k3, uint32_t *r1, uint32_t *r3)
 {
-    // one Philox block of the acceptance stream (k1) and one of the direction
-    // stream (k3) at the same counter (muca_delta_multigpu.cu:794-797)
     const uint4 a = philox<R>(cc, seed, iter, kCtrTag, k1);
     const uint4 b = philox<R>(cc, seed, iter, kCtrTag, k3);
-    p[0] = pack_draw(a.x, b.x);
-    p[1] = pack_draw(a.y, b.y);
-    p[2] = pack_draw(a.z, b.z);
-    p[3] = pack_draw(a.w, b.w);
+    r1[0] = a.x; r1[1] = a.y; r1[2] = a.z; r1[3] = a.w;
+    r3[0] = b.x; r3[1] = b.y; r3[2] = b.z; r3[3] = b.w;
 }
+
 
 // Histogram entry.  The u32 shared bins are drained into the u64 device
 // histogram by the lane whose increment finds 2^31 counts already there.
@@ -140,7 +141,8 @@ struct WinDec {
 };
 
 // Decodes the SLOTS same-parity sites (half 0: even, 1: odd) of word q of
-// row `row`, SLOTS consecutive attempts of the sweep, with packed draws p[].
+// row `row`, SLOTS consecutive attempts of the sweep, with the acceptance
+// words r1[] and direction words r3[] of draw_pair.
 // lat points at this lane's word 0 (stride cpb).  The half is a value, not a
 // template branch, so decode and scan of neighbouring windows form one basic
 // block the compiler can interleave.
@@ -149,8 +151,8 @@ struct WinDec {
 // which for beta = 2 is the same value.
 template <int MODE, int SLOTS, bool BT = false>
 __device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
-                                              uint32_t row, uint32_t q, uint32_t half, const uint32_t *p,
-                                              const float *__restrict__ btab, WinDec<MODE> &d)
+                                              uint32_t row, uint32_t q, uint32_t half, const uint32_t *r1,
+                                              const uint32_t *r3, const float *__restrict__ btab, WinDec<MODE> &d)
 {
     using WT = typename WeightType<MODE>::T;
     constexpr uint32_t M2 = 0x33333333u, N1 = 0x11111111u;
@@ -181,7 +183,7 @@ __device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32
     // cyclic wrap is code -> (code + 1 + d) mod 3, d the direction bit.
     uint32_t dn = 0;
 #pragma unroll
-    for (int t = 0; t < SLOTS; ++t) dn |= (p[t] & 1u) << (4 * t);
+    for (int t = 0; t < SLOTS; ++t) dn |= (r3[t] >> 31) << (4 * t);
     const uint32_t x = ctr + N1 + dn;                              // 1..4
     const uint32_t ge3 = ((x + N1) >> 2) & N1;                     // 1 where x >= 3
     const uint32_t vnib = x - (ge3 + (ge3 << 1));                  // new codes 0..2
@@ -202,8 +204,8 @@ __device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32
         d.dM[t] = dv;
         if (BT) d.f2[t] = btab[d.dE[t] + 8];
         else    d.f2[t] = small_int_to_float(-2 * d.dE[t]);
-        d.lf[t] = __logf(u01f(p[t]));
-        d.p[t] = p[t];
+        d.lf[t] = __logf(u01f(r1[t]));
+        d.p[t] = r1[t];
     }
 }
 
@@ -370,13 +372,13 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
                                             uint32_t row, uint32_t q, bool rec, bool store, bool checked,
                                             const typename WeightType<MODE>::T *__restrict__ wS,
                                             uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
-                                            ChainState &st, const uint32_t (&p)[SLOTS],
+                                            ChainState &st, const uint32_t (&r1)[SLOTS], const uint32_t (&r3)[SLOTS],
                                             typename WeightType<MODE>::T eps, const float *__restrict__ btab = nullptr,
                                             uint32_t hrt = 0, const double *__restrict__ wG = nullptr,
                                             float tol = 0.0f)
 {
     WinDec<MODE> d;
-    decode_window<MODE, SLOTS, BT>(lat, cpb, L, WPR, row, q, HALF < 0 ? hrt : (uint32_t)HALF, p, btab, d);
+    decode_window<MODE, SLOTS, BT>(lat, cpb, L, WPR, row, q, HALF < 0 ? hrt : (uint32_t)HALF, r1, r3, btab, d);
     scan_window<MODE, SLOTS, HS>(d, rec, store, checked, wS, histS, histG, st, eps, wG, tol);
 }
 
@@ -587,19 +589,23 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
     // u32 shared bins can overflow only if the launch can record 2^32 entries in one block
     const bool checked = (unsigned long long)cpb * nup >= 0xFFFFFFFFull;
     const uint32_t L = a.L, WPR = a.WPR;
-    uint32_t next[8];
-    draw_group<R>(1u, cs.seed, iter, cs.k1, cs.k3, next);
-    draw_group<R>(2u, cs.seed, iter, cs.k1, cs.k3, next + 4);
+    // draws of the next two groups (counters cc - 1, cc), the two streams apart
+    uint32_t n1[8], n3[8];
+    draw_pair<R>(1u, cs.seed, iter, cs.k1, cs.k3, n1, n3);
+    draw_pair<R>(2u, cs.seed, iter, cs.k1, cs.k3, n1 + 4, n3 + 4);
     uint32_t cc = 2;
     auto advance = [&](uint32_t groups) {
         if (groups == 2) {
-            draw_group<R>(cc + 1, cs.seed, iter, cs.k1, cs.k3, next);
-            draw_group<R>(cc + 2, cs.seed, iter, cs.k1, cs.k3, next + 4);
+            draw_pair<R>(cc + 1, cs.seed, iter, cs.k1, cs.k3, n1, n3);
+            draw_pair<R>(cc + 2, cs.seed, iter, cs.k1, cs.k3, n1 + 4, n3 + 4);
             cc += 2;
         } else {
 #pragma unroll
-            for (int t = 0; t < 4; ++t) next[t] = next[t + 4];
-            draw_group<R>(cc + 1, cs.seed, iter, cs.k1, cs.k3, next + 4);
+            for (int t = 0; t < 4; ++t) {
+                n1[t] = n1[t + 4];
+                n3[t] = n3[t + 4];
+            }
+            draw_pair<R>(cc + 1, cs.seed, iter, cs.k1, cs.k3, n1 + 4, n3 + 4);
             cc += 1;
         }
     };
@@ -607,22 +613,31 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
                                               bool rec_phase) {
         const bool rec = rec_phase && cs.active;
         if (len < cnt) {
-            partial_core<MODE, HS, BT>(lat, cpb, L, WPR, row, q, half, len, rec, store, wP, histS, a.hist, st, next, btab);
-            advance((len + 3u) >> 2);
-        } else if (cnt == 8) {
             uint32_t p[8];
 #pragma unroll
-            for (int t = 0; t < 8; ++t) p[t] = next[t];
-            advance(2);  // independent of the window below: overlaps its scan
-            window_core<MODE, 8, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p,
-                                             eps, btab, half, wG, tol);
-        } else {
-            uint32_t p[4];
+            for (int t = 0; t < 8; ++t) p[t] = pack_draw(n1[t], n3[t]);
+            partial_core<MODE, HS, BT>(lat, cpb, L, WPR, row, q, half, len, rec, store, wP, histS, a.hist, st, p, btab);
+            advance((len + 3u) >> 2);
+        } else if (cnt == 8) {
+            uint32_t r1[8], r3[8];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) p[t] = next[t];
+            for (int t = 0; t < 8; ++t) {
+                r1[t] = n1[t];
+                r3[t] = n3[t];
+            }
+            advance(2);  // independent of the window below: overlaps its scan
+            window_core<MODE, 8, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
+                                             r3, eps, btab, half, wG, tol);
+        } else {
+            uint32_t r1[4], r3[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                r1[t] = n1[t];
+                r3[t] = n3[t];
+            }
             advance(1);
-            window_core<MODE, 4, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, p,
-                                             eps, btab, half, wG, tol);
+            window_core<MODE, 4, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
+                                             r3, eps, btab, half, wG, tol);
         }
         return true;
     });
