@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Benchmark of the multicanonical weight-estimation hot path on GB300.
 
-Metric (the benchmark spec): spin-flip attempts/ns at L=72, one GB300 against the
-host CPU.  One step = one iteration of the reference weight loop
+Metric: spin-flip attempts/ns at L=72, one GB300 against the host CPU.  One
+step = one iteration of the reference weight loop
 (muca_delta_multigpu.cu:374-477) on the workload of the L=72 configuration:
 16384 chains, therm = N = 5184 attempts then nup = N recorded attempts per
 chain (2 * 5184 * 16384 = 169.9 M attempts), followed by the FP64 trivial
@@ -384,7 +384,7 @@ def flat_run_metric(local):
     N = L * L
     with m.Engine(L, nchains=nc, device=local) as e:
         res, _ = e.weight_run(starting_M=N, rule=m.UPDATE_TRIVIAL, nup_schedule=1, flat_minmean=1, max_iter=6000,
-                              nup_max=1 << 20, init_scheme=m.INIT_BASELINE, records=1)
+                              nup_max=1 << 20, init_scheme=m.INIT_CHAIN_COUNTER, records=1)
     return {"metric": "weight iterations to a flat histogram (min/mean >= 0.5) at L=72", "L": L, "chains": nc,
             "iterations": res.iterations, "converged": bool(res.converged),
             "width_reached_iteration": res.width_reached_iter, "device_s": res.total_kernel_s,

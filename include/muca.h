@@ -59,7 +59,7 @@ typedef enum muca_init_scheme {
                                ctr {2*dev, 100, 0xBADCAB1E, 0xBADC0DED}, ++ctr[0] per 4 sites */
     MUCA_INIT_PRODUCE = 1,  /* produce2_multigpu.cu:126-138: key {10W, 0xdecafbad},
                                ctr {1000*dev, 100, 0, 0xBADCAFE3}, ++ctr[2] per 4 sites */
-    MUCA_INIT_BASELINE = 2, /* extension: Philox4x32-10, key {2024, jack}, ctr {chain, group, 0, 0} */
+    MUCA_INIT_CHAIN_COUNTER = 2, /* extension: Philox4x32-10, key {2024, jack}, ctr {chain, group, 0, 0} */
     MUCA_INIT_ORDERED = 3,  /* extension for rand_config=0: every spin +1 */
     MUCA_INIT_MUCA_MAG = 4  /* muca_mag.cpp:63-73 (the CPU weight program): key {10W + 10000*jack,
                                0xdecafbad}, ctr {0, 100, 0xBADCAB1E, 0xBADC0DED}, ++ctr[0] per 4 sites */

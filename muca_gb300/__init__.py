@@ -21,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libmuca.so")
 
 MODE_WEIGHT, MODE_PRODUCE = 0, 1
-INIT_WEIGHT, INIT_PRODUCE, INIT_BASELINE, INIT_ORDERED, INIT_MUCA_MAG = 0, 1, 2, 3, 4
+INIT_WEIGHT, INIT_PRODUCE, INIT_CHAIN_COUNTER, INIT_ORDERED, INIT_MUCA_MAG = 0, 1, 2, 3, 4
 ALGO_SWEEP, ALGO_RANDOM_SITE = 0, 1
 UPDATE_TRIVIAL, UPDATE_TRIVIAL_CPU, UPDATE_RECURSION = 0, 1, 2
 KERNEL_AUTO, KERNEL_GENERIC, KERNEL_WINDOWED, KERNEL_SPECIALIZED = 0, 1, 2, 3

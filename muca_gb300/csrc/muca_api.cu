@@ -405,7 +405,7 @@ muca_status muca_init_chains(muca_ctx *c, uint32_t scheme, uint32_t jack)
         ia.ctr0[1] = 100; ia.ctr0[3] = 0xBADCAFE3u;
         ia.ctr0_dev_mul[0] = 1000; ia.ctr_word = 2;
         break;
-    case MUCA_INIT_BASELINE:
+    case MUCA_INIT_CHAIN_COUNTER:
         ia.key0_add = 2024; ia.key1_jack_mul = 1; ia.rounds = 10; ia.chain_in_ctr = 1;
         break;
     case MUCA_INIT_ORDERED:

@@ -92,7 +92,7 @@ struct InitArgs {
     uint32_t ctr0[4], ctr0_dev_mul[4];
     uint32_t ctr_word;  // counter word incremented before every 4 sites
     uint32_t rounds;
-    uint32_t chain_in_ctr;  // 1: ctr[0] = chain_offset + chain and ctr[1] = group (baseline scheme)
+    uint32_t chain_in_ctr;  // 1: ctr[0] = chain_offset + chain and ctr[1] = group (chain-counter scheme)
     uint32_t chain_offset;
     uint32_t ordered;       // 1: every spin +1
 };

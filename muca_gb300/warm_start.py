@@ -7,7 +7,7 @@ The reference's only alternative to a zero initial weight is an extrapolated
 weight file read by its `continuing` path (muca_delta_multigpu.cu:223-235);
 the prediction takes that place here.  The iteration itself is unchanged:
 same update rule, same schedule, same stop criterion (min/mean >= 0.5), so the
-iteration remains the judge of the surrogate's error.
+iterations it takes measure the surrogate's error.
 
     python -m muca_gb300.warm_start [--L 16,24,32,48] [--chains 1024] ...
 

@@ -503,8 +503,8 @@ void orc_weight_recursion(const uint64_t *hist, unsigned N, double *p_acc, int h
     free(bf);
 }
 
-/* Flatness of the benchmark's criterion: min_i H[i] / mean_i H[i] over all
- * N+1 bins (no reference routine; E_Delta covers every bin of [0,N]).     */
+/* Flatness as min_i H[i] / mean_i H[i] over all N+1 bins (no reference
+ * routine; E_Delta covers every bin of [0,N]).                            */
 void orc_flatness(const uint64_t *h, unsigned N, double *min_over_mean, int *start, int *end)
 {
     uint64_t mn = h[0];
