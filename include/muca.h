@@ -288,7 +288,8 @@ typedef struct muca_instance {
 
 typedef struct muca_batch_shape {
     uint32_t chains_per_block;  /* 32, 64, 128 or 256 */
-    uint32_t lattice_in_smem;   /* packed lattice staged in shared memory */
+    uint32_t lattice_in_smem;   /* packed lattice staged in shared memory: 0 no, 1 yes, 2 for the
+                                   instances whose block fits (global memory for the rest) */
     uint32_t hist_in_smem;      /* u32 histogram bins in shared memory (else u64 device atomics) */
     uint32_t blocks_per_sm;     /* resident blocks of the persistent grid per SM */
     double ms;                  /* autotuner: one sweep (therm N + nup N) of the whole batch */

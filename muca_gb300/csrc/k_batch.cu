@@ -33,10 +33,11 @@ __global__ void k_batch_prep(const BatchInst *__restrict__ insts, uint32_t *__re
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) h[i] = 0ull;
 }
 
-template <int R, bool LAT_SMEM, bool HS>
+template <int R, int LAT, bool HS>
 __global__ void __launch_bounds__(256, 1) k_batch_sweep(const BatchInst *__restrict__ insts,
                                                          const BatchItem *__restrict__ items, uint32_t n_items,
-                                                         uint32_t *__restrict__ next_item, uint32_t cpb)
+                                                         uint32_t *__restrict__ next_item, uint32_t cpb,
+                                                         uint32_t smem_bytes)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t s_item;
@@ -54,7 +55,19 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep(const BatchInst *__restr
         if (launch_params(a, iter, nup)) {  // the instance is still running
             if (threadIdx.x < 17) s_btab[threadIdx.x] = I->btab[threadIdx.x];
             // s_btab is read only after the block barrier inside the sweep's prologue
-            win_sweep_block<kModeWeight, R, LAT_SMEM, HS, true>(a, smem, cpb, item.blk, iter, nup, s_btab);
+            if (LAT == kLatWhereFits) {
+                // uniform per item: the lattice joins the weights (and bins) in
+                // shared memory when all fit in the launch's allocation
+                const size_t need = smem_weights_bytes(kModeWeight, a.N) +
+                                    (HS ? smem_hist_bytes(kModeWeight, a.N) : 0) + (size_t)a.L * a.WPR * 4u * cpb;
+                if (need <= smem_bytes)
+                    win_sweep_block<kModeWeight, R, true, HS, true>(a, smem, cpb, item.blk, iter, nup, s_btab);
+                else
+                    win_sweep_block<kModeWeight, R, false, HS, true>(a, smem, cpb, item.blk, iter, nup, s_btab);
+            } else {
+                win_sweep_block<kModeWeight, R, LAT == kLatShared, HS, true>(a, smem, cpb, item.blk, iter, nup,
+                                                                            s_btab);
+            }
         }
         __syncthreads();
     }
@@ -74,34 +87,44 @@ size_t batch_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem, bool hist_smem)
            (lat_smem ? (size_t)L * WPR * 4 * cpb : 0);
 }
 
-using BatchKernel = void (*)(const BatchInst *, const BatchItem *, uint32_t, uint32_t *, uint32_t);
+using BatchKernel = void (*)(const BatchInst *, const BatchItem *, uint32_t, uint32_t *, uint32_t, uint32_t);
 
-static BatchKernel batch_kernel(int rounds, bool lat_smem, bool hist_smem)
+template <int R, int LAT>
+static BatchKernel batch_kernel_lat(bool hist_smem)
 {
-#define MUCA_PICK(R)                                                                                   \
-    return lat_smem ? (hist_smem ? k_batch_sweep<R, true, true> : k_batch_sweep<R, true, false>)      \
-                    : (hist_smem ? k_batch_sweep<R, false, true> : k_batch_sweep<R, false, false>)
-    if (rounds == 10) MUCA_PICK(10);
-    MUCA_PICK(7);
-#undef MUCA_PICK
+    return hist_smem ? k_batch_sweep<R, LAT, true> : k_batch_sweep<R, LAT, false>;
 }
 
-cudaError_t batch_sweep_occupancy(uint32_t cpb, int rounds, bool lat_smem, bool hist_smem, size_t smem, int *blocks)
+template <int R>
+static BatchKernel batch_kernel_r(uint32_t lat, bool hist_smem)
 {
-    const BatchKernel k = batch_kernel(rounds, lat_smem, hist_smem);
+    return lat == kLatWhereFits ? batch_kernel_lat<R, kLatWhereFits>(hist_smem)
+         : lat == kLatShared    ? batch_kernel_lat<R, kLatShared>(hist_smem)
+                                : batch_kernel_lat<R, kLatGlobal>(hist_smem);
+}
+
+static BatchKernel batch_kernel(int rounds, uint32_t lat, bool hist_smem)
+{
+    return rounds == 10 ? batch_kernel_r<10>(lat, hist_smem) : batch_kernel_r<7>(lat, hist_smem);
+}
+
+cudaError_t batch_sweep_occupancy(uint32_t cpb, int rounds, uint32_t lat, bool hist_smem, size_t smem, int *blocks)
+{
+    if (lat > kLatWhereFits) return cudaErrorInvalidValue;
+    const BatchKernel k = batch_kernel(rounds, lat, hist_smem);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, (int)((cpb + 31u) / 32u * 32u), smem);
 }
 
 cudaError_t launch_batch_sweep(const BatchInst *insts, const BatchItem *items, uint32_t n_items, uint32_t *next_item,
-                               uint32_t cpb, int rounds, bool lat_smem, bool hist_smem, uint32_t grid, size_t smem,
+                               uint32_t cpb, int rounds, uint32_t lat, bool hist_smem, uint32_t grid, size_t smem,
                                cudaStream_t s)
 {
     // the shared-memory attribute was set by batch_sweep_occupancy for this shape
-    if (cpb == 0 || cpb > 256) return cudaErrorInvalidValue;
-    const BatchKernel k = batch_kernel(rounds, lat_smem, hist_smem);
-    k<<<grid, (cpb + 31u) / 32u * 32u, smem, s>>>(insts, items, n_items, next_item, cpb);
+    if (cpb == 0 || cpb > 256 || lat > kLatWhereFits) return cudaErrorInvalidValue;
+    const BatchKernel k = batch_kernel(rounds, lat, hist_smem);
+    k<<<grid, (cpb + 31u) / 32u * 32u, smem, s>>>(insts, items, n_items, next_item, cpb, (uint32_t)smem);
     return cudaGetLastError();
 }
 

@@ -204,12 +204,30 @@ muca_status set_layout(muca_batch *b, uint32_t cpb, uint32_t rule)
     return MUCA_OK;
 }
 
+// Dynamic shared memory a sweep block may use: the device's opt-in limit less
+// a reserve for the kernel's static shared memory.
+size_t smem_budget(const muca_batch *b) { return b->smem_optin > 1024 ? b->smem_optin - 1024 : 0; }
+
+// Launch shared memory of a shape: the largest block over the instances, each
+// with its lattice in shared memory where the shape puts it there
+// (kLatWhereFits: where the block stays within the budget; the sweep kernel
+// makes the same choice per instance against the launch's size).
+size_t shape_smem(const muca_batch *b, uint32_t cpb, uint32_t lat, bool hist_smem)
+{
+    size_t smem = 0;
+    for (const muca_instance &m : b->inst) {
+        const size_t with = batch_sweep_smem(m.L, cpb, true, hist_smem);
+        const size_t without = batch_sweep_smem(m.L, cpb, false, hist_smem);
+        const bool in = lat == kLatShared || (lat == kLatWhereFits && with <= smem_budget(b));
+        smem = std::max(smem, in ? with : without);
+    }
+    return smem;
+}
+
 muca_status apply_shape(muca_batch *b, const muca_batch_shape &s, uint32_t rule)
 {
     if (muca_status st = set_layout(b, s.chains_per_block, rule)) return st;
-    size_t smem = 0;
-    for (const muca_instance &m : b->inst)
-        smem = std::max(smem, batch_sweep_smem(m.L, s.chains_per_block, s.lattice_in_smem, s.hist_in_smem));
+    const size_t smem = shape_smem(b, s.chains_per_block, s.lattice_in_smem, s.hist_in_smem);
     int per_sm = 0;
     BCUDA(b, batch_sweep_occupancy(s.chains_per_block, b->rounds, s.lattice_in_smem, s.hist_in_smem, smem, &per_sm));
     if (per_sm < 1) return bfail(b, MUCA_ERR_BAD_ARG, "shape does not fit on an SM");
@@ -314,11 +332,16 @@ muca_status autotune(muca_batch *b)
     b->tried.clear();
     muca_status rs = MUCA_OK;
     for (uint32_t cpb : cpbs) {
-        for (int ls = 0; ls < 2 && rs == MUCA_OK; ++ls) {
+        for (uint32_t ls = kLatGlobal; ls <= kLatWhereFits && rs == MUCA_OK; ++ls) {
             for (int hs = 0; hs < 2 && rs == MUCA_OK; ++hs) {
-                size_t smem = 0;
-                for (const muca_instance &m : b->inst) smem = std::max(smem, batch_sweep_smem(m.L, cpb, ls, hs));
-                if (smem > b->smem_optin) continue;
+                const size_t smem = shape_smem(b, cpb, ls, hs);
+                if (smem > smem_budget(b)) continue;
+                if (ls == kLatWhereFits) {
+                    // only a mix differs from the all-global and all-shared shapes
+                    uint32_t in = 0;
+                    for (const muca_instance &m : b->inst) in += batch_sweep_smem(m.L, cpb, true, hs) <= smem_budget(b);
+                    if (in == 0 || in == b->n) continue;
+                }
                 muca_batch_shape s{};
                 s.chains_per_block = cpb;
                 s.lattice_in_smem = (uint32_t)ls;
@@ -454,12 +477,15 @@ muca_status muca_batch_create(const muca_batch_params *p, const muca_instance *i
             bfail(b, MUCA_ERR_BAD_ARG, "chains per block %u (32..256, a multiple of 32)", s.chains_per_block);
             return bail(MUCA_ERR_BAD_ARG);
         }
-        size_t smem = 0;
-        for (const muca_instance &m : b->inst)
-            smem = std::max(smem, batch_sweep_smem(m.L, s.chains_per_block, s.lattice_in_smem, s.hist_in_smem));
-        if (smem > b->smem_optin) {
-            bfail(b, MUCA_ERR_BAD_ARG, "shape needs %zu B of shared memory per block (device has %zu)", smem,
-                  b->smem_optin);
+        if (s.lattice_in_smem > kLatWhereFits || s.hist_in_smem > 1) {
+            bfail(b, MUCA_ERR_BAD_ARG, "lattice_in_smem %u (0..2), hist_in_smem %u (0..1)", s.lattice_in_smem,
+                  s.hist_in_smem);
+            return bail(MUCA_ERR_BAD_ARG);
+        }
+        const size_t smem = shape_smem(b, s.chains_per_block, s.lattice_in_smem, s.hist_in_smem);
+        if (smem > smem_budget(b)) {
+            bfail(b, MUCA_ERR_BAD_ARG, "shape needs %zu B of shared memory per block (device allows %zu)", smem,
+                  smem_budget(b));
             return bail(MUCA_ERR_BAD_ARG);
         }
         st = apply_shape(b, s, 0);

@@ -159,18 +159,24 @@ struct BatchItem {
 // Clears the histograms of the running instances and resets the work counter.
 cudaError_t launch_batch_prep(const BatchInst *insts, uint32_t n_inst, uint32_t *next_item, uint32_t *running,
                               cudaStream_t s);
+// Lattice placement of a batch sweep: in global memory, in shared memory,
+// or per instance in shared memory where it fits in the block's `smem`
+// bytes (global memory for the rest).
+enum BatchLattice : uint32_t { kLatGlobal = 0, kLatShared = 1, kLatWhereFits = 2 };
 // Persistent sweep over `items` (fetched through *next_item) with chain
-// blocks of cpb chains; lat_smem / hist_smem select the shared-memory
-// placement.  grid blocks of roundup32(cpb) threads and `smem` bytes.
+// blocks of cpb chains; lat (BatchLattice) / hist_smem select the
+// shared-memory placement.  grid blocks of roundup32(cpb) threads and
+// `smem` bytes.
 cudaError_t launch_batch_sweep(const BatchInst *insts, const BatchItem *items, uint32_t n_items, uint32_t *next_item,
-                               uint32_t cpb, int rounds, bool lat_smem, bool hist_smem, uint32_t grid, size_t smem,
+                               uint32_t cpb, int rounds, uint32_t lat, bool hist_smem, uint32_t grid, size_t smem,
                                cudaStream_t s);
-// Dynamic shared memory of one batch sweep block for an instance of size L.
+// Dynamic shared memory of one batch sweep block for an instance of size L,
+// with or without its lattice.
 size_t batch_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem, bool hist_smem);
 // Blocks of the batch sweep that fit on one SM with `smem` bytes each; also
 // sets the kernel's shared-memory limit to `smem` (call before any capture).
 // The launch with that shape needs no further attribute call.
-cudaError_t batch_sweep_occupancy(uint32_t cpb, int rounds, bool lat_smem, bool hist_smem, size_t smem, int *blocks);
+cudaError_t batch_sweep_occupancy(uint32_t cpb, int rounds, uint32_t lat, bool hist_smem, size_t smem, int *blocks);
 // Sets the update kernel's shared-memory limit (call before any capture).
 cudaError_t prepare_batch_update(uint32_t max_N, int any_recursion);
 // The update step of every instance; *running += instances not stopped.

@@ -51,6 +51,28 @@ def test_batch_equals_single_simulations(muca, shape):
         np.testing.assert_array_equal(hs[i], h, err_msg="instance %d" % i)
 
 
+# lattice placement 2: in shared memory for the instances whose block fits
+# (L = 16 and 72 here), in global memory for the rest (L = 128)
+MIXED = [(128, 64, 2.0, 5), (16, 256, 2.0, 0), (72, 128, 2.0, 6)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(128, 2, 1), (64, 2, 0)], ids=lambda s: "cpb%d_lat%d_hist%d" % s)
+def test_batch_lattice_where_it_fits_equals_single_simulations(muca, shape):
+    kw = dict(flat_minmean=1, max_iter=12)
+    with muca.Batch(MIXED, shape=shape) as b:
+        res, _ = b.run(starting_M=1, graph_iters=4, **kw)
+        ws = [b.get_weights(i) for i in range(len(MIXED))]
+        hs = [b.histogram(i) for i in range(len(MIXED))]
+        info = b.info()
+    assert (info.shape.chains_per_block, info.shape.lattice_in_smem, info.shape.hist_in_smem) == shape
+    for i, (L, nc, beta, seed) in enumerate(MIXED):
+        r, w, h = _single(muca, L, nc, seed, **kw)
+        assert (res[i].iterations, res[i].total_run) == (r.iterations, r.total_run), i
+        np.testing.assert_array_equal(ws[i], w, err_msg="instance %d" % i)
+        np.testing.assert_array_equal(hs[i], h, err_msg="instance %d" % i)
+
+
 @pytest.mark.gpu
 def test_batch_recursion_doubling_equals_single_simulations(muca):
     kw = dict(rule=muca.UPDATE_RECURSION, nup_schedule=1, flat_minmean=1, max_iter=40)
