@@ -219,6 +219,17 @@ muca_status muca_set_histogram(muca_ctx *ctx, const uint64_t *h, size_t n);
 muca_status muca_histogram_stats(muca_ctx *ctx, muca_hist_stats *stats);
 muca_status muca_update_weights(muca_ctx *ctx, uint32_t rule, muca_hist_stats *stats);
 
+/* One iteration of the reference's weight loop with host buffers, as one
+ * call with one host synchronisation (muca_delta_multigpu.cu:384-476):
+ * lnw_in (N+1 values; NULL keeps the device weights) as muca_set_weights,
+ * one sweep as muca_sweep, the update `rule` as muca_update_weights, then
+ * the updated weights into lnw_out and the sweep's histogram into hist_out
+ * (N+1 each; either may be NULL) and, if stats is not NULL, the histogram
+ * summary.  Weight mode only.  The same results as the five separate calls. */
+muca_status muca_iterate_host(muca_ctx *ctx, const double *lnw_in, uint32_t iter, uint32_t seed_base,
+                              uint32_t seed_dev_mul, uint64_t therm, uint64_t nup, uint32_t rule,
+                              double *lnw_out, uint64_t *hist_out, muca_hist_stats *stats);
+
 /* Full weight-estimation run of one jack (muca_delta_multigpu.cu:329-477).
  * recs (optional, capacity cap) receives one record per iteration. */
 muca_status muca_weight_run(muca_ctx *ctx, const muca_run_opts *opts, muca_run_result *res,

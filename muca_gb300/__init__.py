@@ -33,6 +33,7 @@ EXPORTS = [
     "muca_init_chains", "muca_set_lattice", "muca_get_lattice", "muca_get_chain_state",
     "muca_set_weights", "muca_get_weights", "muca_sweep", "muca_sweep_accumulate",
     "muca_clear_histogram", "muca_get_histogram", "muca_set_histogram", "muca_histogram_stats", "muca_update_weights",
+    "muca_iterate_host",
     "muca_weight_run", "muca_weight_shift", "muca_compute_observables", "muca_jackknife",
     "muca_philox_peak", "muca_weight_run_stream", "muca_get_reweighting_weights",
     "muca_observables_noalloc",
@@ -173,6 +174,8 @@ def lib():
     L.muca_set_histogram.argtypes = [vp, u64, C.c_size_t]
     L.muca_histogram_stats.argtypes = [vp, C.POINTER(HistStats)]
     L.muca_update_weights.argtypes = [vp, C.c_uint32, C.POINTER(HistStats)]
+    L.muca_iterate_host.argtypes = [vp, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint64,
+                                    C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(HistStats)]
     L.muca_weight_run.argtypes = [vp, C.POINTER(RunOpts), C.POINTER(RunResult), C.POINTER(IterRecord), C.c_size_t]
     L.muca_weight_shift.argtypes = [vp, C.c_double, C.c_double]
     L.muca_get_reweighting_weights.argtypes = [vp, f64, C.c_size_t]
@@ -338,6 +341,26 @@ class Engine:
             return None
         s = HistStats()
         self._ck(self._lib.muca_update_weights(self._h, rule, C.byref(s)))
+        return s
+
+    def iterate_host(self, lnw_in, iter, seed_base, seed_dev_mul, therm, nup, rule=UPDATE_TRIVIAL, lnw_out=None,
+                     hist_out=None, stats=False):
+        """One weight iteration with host buffers and one synchronisation:
+        weights in (None keeps the device's), sweep, update, then the updated
+        weights and the histogram into the given float64 / uint64 arrays of
+        N+1 (either may be None).  Returns the histogram summary if stats."""
+        n = self.N + 1
+
+        def arr(a, dt):
+            if a is None:
+                return None
+            if a.dtype != dt or a.size != n or not a.flags.c_contiguous:
+                raise ValueError("expected a contiguous %s array of %d values" % (dt, n))
+            return a.ctypes.data
+        s = HistStats() if stats else None
+        self._ck(self._lib.muca_iterate_host(self._h, arr(lnw_in, np.float64), iter, seed_base, seed_dev_mul,
+                                             therm, nup, rule, arr(lnw_out, np.float64),
+                                             arr(hist_out, np.uint64), C.byref(s) if stats else None))
         return s
 
     def weight_run(self, starting_M=1, jack=0, rule=UPDATE_TRIVIAL, hold_until_full=0, flat_minmean=0,

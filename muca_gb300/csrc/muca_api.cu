@@ -581,6 +581,34 @@ muca_status muca_update_weights(muca_ctx *c, uint32_t rule, muca_hist_stats *st)
     return update_impl(c, (int)rule, st);
 }
 
+muca_status muca_iterate_host(muca_ctx *c, const double *lnw_in, uint32_t iter, uint32_t seed_base,
+                              uint32_t seed_dev_mul, uint64_t therm, uint64_t nup, uint32_t rule, double *lnw_out,
+                              uint64_t *hist_out, muca_hist_stats *st)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "iterate_host needs a weight-mode context");
+    if (rule > MUCA_UPDATE_RECURSION) return fail(c, MUCA_ERR_BAD_ARG, "rule %u", rule);
+    const size_t n = (size_t)c->N + 1;
+    if (lnw_in)
+        for (size_t i = 0; i < n; ++i)
+            if (!std::isfinite(lnw_in[i])) return fail(c, MUCA_ERR_BAD_ARG, "weight %zu is not finite", i);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (lnw_in) {
+        // read by the stream before this call returns (it synchronises below)
+        CUDA_TRY(c, cudaMemcpyAsync(c->d_lnw, lnw_in, n * 8, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(c->d_lnw_obs, c->d_lnw, n * 8, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(c, launch_weights_to_f32(c->d_lnw, c->d_w32, (uint32_t)n, c->stream));
+    }
+    if (muca_status e = do_sweep(c, iter, seed_base, seed_dev_mul, therm, nup, true)) return e;
+    CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, (int)rule, c->d_stats, c->stream));
+    if (st) CUDA_TRY(c, cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(HistStatsDev), cudaMemcpyDeviceToHost, c->stream));
+    if (lnw_out) CUDA_TRY(c, cudaMemcpyAsync(lnw_out, c->d_lnw, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (hist_out) CUDA_TRY(c, cudaMemcpyAsync(hist_out, c->d_hist, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (muca_status e = check_err(c)) return e;  // the one synchronisation
+    if (st) stats_out(*c->h_stats, st);
+    return MUCA_OK;
+}
+
 static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result *res, muca_iter_record *recs,
                             size_t cap, muca_iter_callback cb, void *user)
 {

@@ -465,3 +465,37 @@ def test_full_size_L72_properties(muca, orc, kernel):
         orc.weight_sweep(L, a, ej, ed, lnw.astype(np.float32), 7, SEED, N, 2 * N + 8, chain0=lo, nthreads=8)
         np.testing.assert_array_equal(lat1[lo:hi], a.reshape(hi - lo, N))
         np.testing.assert_array_equal(ed1[lo:hi], ed)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rule", [0, 2])
+def test_iterate_host_equals_separate_calls(muca, rule):
+    """muca_iterate_host (weights in, sweep, update, weights and histogram out,
+    one synchronisation) gives what the five separate calls give."""
+    L, nc = 16, 256
+    N = L * L
+    rng = np.random.default_rng(3)
+    w0 = np.cumsum(rng.normal(-0.5, 0.3, N + 1))
+    w0 -= w0[0]
+    runs = []
+    for fused in (False, True):
+        out = []
+        with muca.Engine(L, nchains=nc) as e:
+            e.init_chains(muca.INIT_WEIGHT, 0)
+            w = w0.copy()
+            for k in range(3):
+                if fused:
+                    wo, ho = np.zeros(N + 1), np.zeros(N + 1, np.uint64)
+                    s = e.iterate_host(w, k, 100, 1000, N, 2 * N, rule, lnw_out=wo, hist_out=ho, stats=True)
+                else:
+                    e.set_weights(w)
+                    e.sweep(k, 100, 1000, N, 2 * N)
+                    s = e.update_weights(rule)
+                    wo, ho = e.get_weights(), e.histogram()
+                out.append((wo.copy(), ho.copy(), (s.start, s.end, s.width, s.events, s.d_kl)))
+                w = wo
+        runs.append(out)
+    for (wa, ha, sa), (wb, hb, sb) in zip(*runs):
+        np.testing.assert_array_equal(wa, wb)
+        np.testing.assert_array_equal(ha, hb)
+        assert sa == sb
