@@ -102,12 +102,15 @@ __global__ void __launch_bounds__(kObsThreads) k_observables(const unsigned long
             for (int k = 0; k < kObsUnroll; ++k) {
                 const unsigned long long H = h[k];
                 const int m = 2 * (int)(j0 + ln + 32u * k) - (int)i;
-                const unsigned long long am = (unsigned long long)(m < 0 ? -m : m);  // <= N <= 16384
-                const unsigned long long am2 = am * am;
+                const uint32_t am = (uint32_t)(m < 0 ? -m : m);  // <= N <= 16384
+                const uint32_t am2 = am * am;                    // < 2^29
+                // 64 x 32-bit products; H m^4 = (H m^2) m^2 with H m^2 < 2^93
+                const u128 t = (u128)H * am2;
+                const unsigned long long tl = (unsigned long long)t, th = (unsigned long long)(t >> 64);
                 a0 += H;
                 a1 += (u128)H * am;
-                a2 += (u128)H * am2;
-                a4 += (u128)H * (am2 * am2);
+                a2 += t;
+                a4 += (u128)tl * am2 + ((u128)(th * am2) << 64);
             }
 #pragma unroll
             for (int k = 0; k < kObsUnroll; ++k) h[k] = hn[k];
