@@ -61,6 +61,9 @@ typedef enum muca_init_scheme {
                                ctr {1000*dev, 100, 0, 0xBADCAFE3}, ++ctr[2] per 4 sites */
     MUCA_INIT_CHAIN_COUNTER = 2, /* extension: Philox4x32-10, key {2024, jack}, ctr {chain, group, 0, 0} */
     MUCA_INIT_ORDERED = 3,  /* extension for rand_config=0: every spin +1 */
+    MUCA_INIT_GRADED = 5,   /* extension: the Philox words of MUCA_INIT_WEIGHT, each spin nonzero with
+                               probability (2W+1)/(2 nchains-per-device) (sign from the word's bit 0),
+                               so the chains' E_Delta cover [0, N] evenly from the start */
     MUCA_INIT_MUCA_MAG = 4  /* muca_mag.cpp:63-73 (the CPU weight program): key {10W + 10000*jack,
                                0xdecafbad}, ctr {0, 100, 0xBADCAB1E, 0xBADC0DED}, ++ctr[0] per 4 sites */
 } muca_init_scheme;
@@ -338,7 +341,8 @@ typedef struct muca_batch_run_opts {
     double d_kl_max;        /* 0 = 1e-4 */
     uint32_t starting_sweeps; /* nonzero: instance i starts at NUPDATES = starting_sweeps * N_i
                                  (replaces starting_M) */
-    uint32_t reserved;
+    uint32_t graded_init;   /* with reinit_chains: 1 = MUCA_INIT_GRADED spins (chains spread over
+                               E_Delta), 0 = the reference's initial spins */
 } muca_batch_run_opts;
 
 typedef struct muca_batch_result {

@@ -21,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libmuca.so")
 
 MODE_WEIGHT, MODE_PRODUCE = 0, 1
-INIT_WEIGHT, INIT_PRODUCE, INIT_CHAIN_COUNTER, INIT_ORDERED, INIT_MUCA_MAG = 0, 1, 2, 3, 4
+INIT_WEIGHT, INIT_PRODUCE, INIT_CHAIN_COUNTER, INIT_ORDERED, INIT_MUCA_MAG, INIT_GRADED = 0, 1, 2, 3, 4, 5
 ALGO_SWEEP, ALGO_RANDOM_SITE = 0, 1
 UPDATE_TRIVIAL, UPDATE_TRIVIAL_CPU, UPDATE_RECURSION = 0, 1, 2
 KERNEL_AUTO, KERNEL_GENERIC, KERNEL_WINDOWED, KERNEL_SPECIALIZED = 0, 1, 2, 3
@@ -124,7 +124,7 @@ class BatchRunOpts(C.Structure):
     _fields_ = [("starting_M", C.c_uint32), ("rule", C.c_uint32), ("nup_schedule", C.c_uint32),
                 ("flat_minmean", C.c_uint32), ("max_iter", C.c_uint32), ("graph_iters", C.c_uint32),
                 ("reinit_chains", C.c_uint32), ("nup_max", C.c_uint32), ("min_over_mean", C.c_double),
-                ("d_kl_max", C.c_double), ("starting_sweeps", C.c_uint32), ("reserved", C.c_uint32)]
+                ("d_kl_max", C.c_double), ("starting_sweeps", C.c_uint32), ("graded_init", C.c_uint32)]
 
 
 class BatchResult(C.Structure):
@@ -469,12 +469,13 @@ class Batch:
         return a
 
     def run(self, starting_M=1, rule=UPDATE_TRIVIAL, nup_schedule=0, flat_minmean=0, max_iter=0, graph_iters=0,
-            reinit_chains=0, min_over_mean=0.0, d_kl_max=0.0, nup_max=0, starting_sweeps=0,
+            reinit_chains=0, min_over_mean=0.0, d_kl_max=0.0, nup_max=0, starting_sweeps=0, graded_init=0,
             raise_on_not_converged=False):
         """Returns (list of BatchResult, device seconds)."""
         o = BatchRunOpts(starting_M=starting_M, rule=rule, nup_schedule=nup_schedule, flat_minmean=flat_minmean,
                          max_iter=max_iter, graph_iters=graph_iters, reinit_chains=reinit_chains, nup_max=nup_max,
-                         min_over_mean=min_over_mean, d_kl_max=d_kl_max, starting_sweeps=starting_sweeps)
+                         min_over_mean=min_over_mean, d_kl_max=d_kl_max, starting_sweeps=starting_sweeps,
+                         graded_init=graded_init)
         res = (BatchResult * len(self.instances))()
         sec = C.c_double()
         self._ck(self._lib.muca_batch_run(self._h, C.byref(o), res, C.byref(sec)),

@@ -61,7 +61,8 @@ __global__ void k_init(uint32_t *lat, uint32_t L, uint32_t WPR, uint32_t cpb, ui
                                             : init_block<7>(ia, W, dev, chain, jack, g);
                         g_cur = g;
                     }
-                    s = init_spin(pick(r, (int)(site & 3u)));
+                    const uint32_t rw = pick(r, (int)(site & 3u));
+                    s = ia.graded ? graded_spin(rw, W, chains_per_dev) : init_spin(rw);
                 }
                 word |= (uint32_t)(s + 1) << (2u * (col - c_lo));
             }

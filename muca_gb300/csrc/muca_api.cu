@@ -396,9 +396,11 @@ muca_status muca_init_chains(muca_ctx *c, uint32_t scheme, uint32_t jack)
     ia.rounds = 7;
     switch (scheme) {
     case MUCA_INIT_WEIGHT:  // muca_delta_multigpu.cu:342-347
+    case MUCA_INIT_GRADED:
         ia.key0_mul = 10; ia.key0_jack_mul = 2; ia.key1 = 0xdecafbadu;
         ia.ctr0[1] = 100; ia.ctr0[2] = 0xBADCAB1Eu; ia.ctr0[3] = 0xBADC0DEDu;
         ia.ctr0_dev_mul[0] = 2; ia.ctr_word = 0;
+        ia.graded = scheme == MUCA_INIT_GRADED;
         break;
     case MUCA_INIT_PRODUCE:  // produce2_multigpu.cu:129-134
         ia.key0_mul = 10; ia.key1 = 0xdecafbadu;

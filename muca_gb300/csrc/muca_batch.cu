@@ -244,8 +244,9 @@ muca_status apply_shape(muca_batch *b, const muca_batch_shape &s, uint32_t rule)
 }
 
 // Reference weight-program initial spins (muca_delta_multigpu.cu:340-351)
-// with emulated device index = seed, then E_J and E_Delta.
-muca_status init_chains(muca_batch *b)
+// with emulated device index = seed, then E_J and E_Delta; graded: the same
+// Philox words through graded_spin (MUCA_INIT_GRADED).
+muca_status init_chains(muca_batch *b, bool graded = false)
 {
     for (uint32_t i = 0; i < b->n; ++i) {
         const muca_instance &m = b->inst[i];
@@ -255,6 +256,7 @@ muca_status init_chains(muca_batch *b)
         ia.ctr0[0] = 2u * m.seed; ia.ctr0[1] = 100; ia.ctr0[2] = 0xBADCAB1Eu; ia.ctr0[3] = 0xBADC0DEDu;
         ia.ctr0_dev_mul[0] = 2; ia.ctr_word = 0;
         ia.chain_offset = m.seed * m.nchains;
+        ia.graded = graded ? 1u : 0u;
         const uint32_t cpb = b->shape.chains_per_block;
         uint32_t *lat = b->d_lat + b->off_lat[i];
         BCUDA(b, launch_init(lat, m.L, wpr_of(m.L), cpb, m.nchains, m.nchains, 0, ia, b->stream));
@@ -585,8 +587,9 @@ muca_status muca_batch_run(muca_batch *b, const muca_batch_run_opts *o, muca_bat
     const uint32_t K = o->graph_iters ? o->graph_iters : 16u;
     if (K > 4096) return bfail(b, MUCA_ERR_BAD_ARG, "graph_iters=%u (at most 4096)", K);
     BCUDA(b, cudaSetDevice(b->device));
+    if (o->graded_init > 1) return bfail(b, MUCA_ERR_BAD_ARG, "graded_init %u (0..1)", o->graded_init);
     if (o->reinit_chains) {
-        if (muca_status st = init_chains(b)) return st;
+        if (muca_status st = init_chains(b, o->graded_init != 0)) return st;
     }
     // the instance table carries the update rule
     if (muca_status st = set_layout(b, b->shape.chains_per_block, o->rule)) return st;

@@ -82,6 +82,16 @@ __device__ __forceinline__ int init_spin(uint32_t r)
     return (u < 1.0 / 3.0) + (u < 2.0 / 3.0) - 1;
 }
 
+// Graded initial spin of worker W of `cpd` (an extension): nonzero with
+// probability (2W + 1) / (2 cpd), decided exactly in integers on the top 24
+// bits of r, with the sign from bit 0, so the workers' E_Delta = sum s^2
+// spread evenly over [0, N] instead of clustering at 2N/3.
+__device__ __forceinline__ int graded_spin(uint32_t r, uint32_t W, uint32_t cpd)
+{
+    const bool nz = (unsigned long long)(r >> 8) * (2ull * cpd) < ((2ull * W + 1ull) << 24);
+    return nz ? ((r & 1u) ? 1 : -1) : 0;
+}
+
 // Packed lattice: 2 bits per site holding s+1 in {0,1,2}; a row of L sites is
 // stored in WPR = ceil(L/16) 32-bit words (site col at bits 2*(col%16) of
 // word col/16).  Device layout [block][row*WPR + word][lane]: the 32 lanes of

@@ -95,6 +95,7 @@ struct InitArgs {
     uint32_t chain_in_ctr;  // 1: ctr[0] = chain_offset + chain and ctr[1] = group (chain-counter scheme)
     uint32_t chain_offset;
     uint32_t ordered;       // 1: every spin +1
+    uint32_t graded;        // 1: graded_spin of the same Philox words instead of init_spin
 };
 cudaError_t launch_init(uint32_t *lat, uint32_t L, uint32_t WPR, uint32_t cpb, uint32_t nchains,
                         uint32_t chains_per_dev, uint32_t jack, const InitArgs &ia, cudaStream_t s);

@@ -128,19 +128,29 @@ def interpolated_weight(L, T, sources, knots=None):
     return out - out.mean()
 
 
-def ab_test(net, held, opts=RUN_OPTS, device=0, sources=None):
+def ab_test(net, held, opts=RUN_OPTS, device=0, sources=None, graded=False):
     """The zero weight against the network's weight on the same held-out
     instances (same seeds, same options).  With `sources` ([(L, T, lnW)],
     the converged training weights) two non-learned arms run beside them:
     "pl", the reference's piecewise-linear form (knots PL_KNOTS) with knot
     heights interpolated in T, and "interp", the full converged weights
-    interpolated in T."""
+    interpolated in T.  With `graded`, the zero, network and interp arms run
+    once more from graded initial spins ("<arm>_g": the chains' E_Delta
+    spread over [0, N] as a converged multicanonical ensemble would hold
+    them, MUCA_INIT_GRADED) instead of the reference's initial spins."""
     arms = {"mlp": [net.log_weights(L, T, D) for L, _, T, D, _ in held]}
     if sources is not None:
         arms["pl"] = [interpolated_weight(L, T, sources, PL_KNOTS) for L, _, T, _, _ in held]
         arms["interp"] = [interpolated_weight(L, T, sources) for L, _, T, _, _ in held]
     rz, sz, wz = converge(held, opts, None, device)
     runs = {k: converge(held, opts, w, device)[:2] for k, w in arms.items()}
+    if graded:
+        og = dict(opts, reinit_chains=1, graded_init=1)
+        runs["zero_g"] = converge(held, og, None, device)[:2]
+        arms["zero_g"] = [np.zeros_like(w) for w in wz]
+        for k in [k for k in ("mlp", "interp") if k in arms]:
+            runs[k + "_g"] = converge(held, og, arms[k], device)[:2]
+            arms[k + "_g"] = arms[k]
     rows = []
     for i, (L, nc, T, D, seed) in enumerate(held):
         row = {"L": L, "T": T, "delta": D, "chains": nc, "zero_iters": rz[i].iterations,
@@ -172,6 +182,7 @@ def main(argv=None):
     p.add_argument("--t-step", type=float, default=0.025)
     p.add_argument("--held-T", default="0.53,0.67")
     p.add_argument("--held-L", default="", help="held-out lattice sizes beyond the training ones")
+    p.add_argument("--graded", action="store_true", help="also run the arms from graded initial spins")
     p.add_argument("--steps", type=int, default=10000, help="Adam steps per learning-rate stage (3 stages)")
     p.add_argument("--schedule", type=int, default=RUN_OPTS["nup_schedule"])
     p.add_argument("--device", type=int, default=0)
@@ -199,7 +210,7 @@ def main(argv=None):
         held = [(L, a.chains, float(T), float(rng.uniform(1.5, 1.99)), 5000 + k)
                 for k, (L, T) in enumerate([(L, float(T)) for L in Ls + held_L for T in a.held_T.split(",")])]
         sources = [(train_inst[i][0], train_inst[i][2], W[i]) for i in ok]
-        ab = ab_test(net, held, opts, a.device, sources)
+        ab = ab_test(net, held, opts, a.device, sources, graded=a.graded)
     out = {"run_opts": {k: v for k, v in opts.items()}, "training_set": gen, "fit": fit, "ab": ab}
     print(json.dumps(out))
     return out

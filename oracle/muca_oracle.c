@@ -120,6 +120,30 @@ void orc_init_lattice(unsigned L, unsigned chain0, unsigned nchains, const orc_i
     }
 }
 
+/* Graded initial spins (an extension of this project, no reference
+ * counterpart): the Philox words of orc_init_lattice, each spin nonzero iff
+ * (r >> 8) * 2 cpd < (2W + 1) * 2^24, the sign from bit 0 of r (1: +1). */
+void orc_init_lattice_graded(unsigned L, unsigned chain0, unsigned nchains, unsigned cpd, const orc_init_scheme *s,
+                             int8_t *lat)
+{
+    unsigned N = L * L;
+    for (unsigned c = 0; c < nchains; c++) {
+        unsigned W = chain0 + c;
+        uint32_t key[2] = {s->key0_mul * W + s->key0_add, s->key1};
+        uint32_t ctr[4] = {s->ctr0[0], s->ctr0[1], s->ctr0[2], s->ctr0[3]};
+        uint32_t r[4] = {0, 0, 0, 0};
+        for (unsigned i = 0; i < N; i++) {
+            if (i % 4 == 0) {
+                ++ctr[s->ctr_word];
+                orc_philox4x32(s->rounds, ctr, key, r);
+            }
+            uint32_t w = r[i % 4];
+            int nz = (uint64_t)(w >> 8) * (2ull * cpd) < ((2ull * W + 1ull) << 24);
+            lat[(size_t)c * N + i] = (int8_t)(nz ? ((w & 1u) ? 1 : -1) : 0);
+        }
+    }
+}
+
 /* total_energy (muca_delta_multigpu.cu:548-571): sum_i -s_i * sum(nb) >> 1 */
 void orc_chain_energies(unsigned L, unsigned nchains, const int8_t *lat, int32_t *ej, int32_t *edel, int32_t *mag)
 {

@@ -53,6 +53,8 @@ orc_init_scheme orc_scheme_produce_cpu(unsigned l);
 /* scheme of muca_mag.cpp:63-73 (CPU weight, jack mm) */
 orc_init_scheme orc_scheme_muca_mag(unsigned jack);
 void orc_init_lattice(unsigned L, unsigned chain0, unsigned nchains, const orc_init_scheme *s, int8_t *lat);
+void orc_init_lattice_graded(unsigned L, unsigned chain0, unsigned nchains, unsigned cpd, const orc_init_scheme *s,
+                             int8_t *lat);
 
 /* E_J (computeEnergies, :69-74 + :548-571), E_Delta (:76-83), M (produce2:84-89) */
 void orc_chain_energies(unsigned L, unsigned nchains, const int8_t *lat, int32_t *ej, int32_t *edel, int32_t *mag);

@@ -76,6 +76,7 @@ def lib():
         getattr(L, n).argtypes = [C.c_uint]
         getattr(L, n).restype = InitScheme
     L.orc_init_lattice.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.POINTER(InitScheme), _i8p]
+    L.orc_init_lattice_graded.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.POINTER(InitScheme), _i8p]
     L.orc_chain_energies.argtypes = [C.c_uint, C.c_uint, _i8p, _i32p, _i32p, _i32p]
     L.orc_weight_sweep.argtypes = [C.c_uint, C.c_uint, C.c_uint, _i8p, _i32p, _i32p, _f32p, _u64p,
                                    C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint, C.c_int]
@@ -156,6 +157,14 @@ def tables(L):
 def init_lattice(L, nchains, scheme, chain0=0):
     lat = np.zeros(nchains * L * L, np.int8)
     lib().orc_init_lattice(L, chain0, nchains, C.byref(scheme), lat)
+    return lat.reshape(nchains, L * L)
+
+
+def init_lattice_graded(L, nchains, scheme, cpd, chain0=0):
+    """The graded initial spins (an extension): worker W of cpd nonzero with
+    probability (2W+1)/(2 cpd), from the same Philox words as init_lattice."""
+    lat = np.zeros(nchains * L * L, np.int8)
+    lib().orc_init_lattice_graded(L, chain0, nchains, cpd, C.byref(scheme), lat)
     return lat.reshape(nchains, L * L)
 
 

@@ -74,6 +74,25 @@ def test_batch_lattice_where_it_fits_equals_single_simulations(muca, shape):
 
 
 @pytest.mark.gpu
+def test_batch_graded_init_equals_single_simulations(muca):
+    """graded_init = 1 with reinit_chains: instance i starts from the
+    MUCA_INIT_GRADED spins of a single context with dev_offset = seed."""
+    kw = dict(flat_minmean=1, max_iter=20)
+    inst = INSTANCES[:3]
+    with muca.Batch(inst) as b:
+        res, _ = b.run(starting_M=1, graph_iters=4, reinit_chains=1, graded_init=1, **kw)
+        ws = [b.get_weights(i) for i in range(len(inst))]
+        hs = [b.histogram(i) for i in range(len(inst))]
+    for i, (L, nc, beta, seed) in enumerate(inst):
+        with muca.Engine(L, nchains=nc, dev_offset=seed) as e:
+            r, _ = e.weight_run(starting_M=1, records=1, init_scheme=muca.INIT_GRADED, **kw)
+            w, h = e.get_weights(), e.histogram()
+        assert (res[i].iterations, res[i].total_run) == (r.iterations, r.total_run), i
+        np.testing.assert_array_equal(ws[i], w, err_msg="instance %d" % i)
+        np.testing.assert_array_equal(hs[i], h, err_msg="instance %d" % i)
+
+
+@pytest.mark.gpu
 def test_batch_recursion_doubling_equals_single_simulations(muca):
     kw = dict(rule=muca.UPDATE_RECURSION, nup_schedule=1, flat_minmean=1, max_iter=40)
     inst = INSTANCES[:3]

@@ -74,6 +74,25 @@ def test_init_produce_scheme(muca, orc, L, cpd, ndev):
     np.testing.assert_array_equal(lat, exp)
 
 
+@pytest.mark.parametrize("L,cpd,ndev,jack", [(16, 256, 2, 0), (24, 100, 1, 3), (72, 64, 1, 0)])
+def test_init_graded_scheme(muca, orc, L, cpd, ndev, jack):
+    """MUCA_INIT_GRADED: the weight scheme's Philox words, worker W's spins
+    nonzero with probability (2W+1)/(2 cpd); E_Delta spreads over [0, N]."""
+    with muca.Engine(L, nchains=cpd, ndev=ndev) as e:
+        e.init_chains(muca.INIT_GRADED, jack)
+        lat = e.get_lattice()
+        ej, ed, mg = e.chain_state()
+    exp = np.concatenate([orc.init_lattice_graded(L, cpd, orc.scheme_weight(jack, d), cpd) for d in range(ndev)])
+    np.testing.assert_array_equal(lat, exp)
+    oj, od, om = orc.energies(L, exp)
+    np.testing.assert_array_equal(ej, oj)
+    np.testing.assert_array_equal(ed, od)
+    N = L * L
+    frac = od[:cpd] / N
+    target = (np.arange(cpd) + 0.5) / cpd
+    assert np.abs(frac - target).max() < 5.0 / np.sqrt(N)
+
+
 def test_set_get_lattice_roundtrip(muca, orc):
     rng = np.random.default_rng(5)
     for L in (3, 16, 72):
