@@ -331,7 +331,8 @@ typedef struct muca_batch_run_opts {
     uint32_t rule;          /* muca_update_rule */
     uint32_t nup_schedule;  /* 0: (NUP+1)*1.01 once width == N (:379-382); 1: doubling once width == N;
                                2: doubling every iteration (cap 2^30); 3: as 0, doubling once every
-                               bin also holds >= 5 % of the mean count */
+                               bin also holds >= 5 % of the mean count; 4: NUP*1.05 every iteration,
+                               the first included (muca_mag.cpp:131) */
     uint32_t flat_minmean;  /* 0: stop at width == N && D_KL < d_kl_max; 1: at min/mean >= min_over_mean */
     uint32_t max_iter;      /* per instance (0 = 1000000) */
     uint32_t graph_iters;   /* iterations per captured graph (0 = 16) */

@@ -278,6 +278,13 @@ std::vector<RunCtl> make_ctl(const muca_batch *b, const muca_batch_run_opts *o)
         const uint32_t N = m.L * m.L;
         c.st.k = 0;
         c.st.nup = o->starting_sweeps ? o->starting_sweeps * N : o->starting_M;
+        if (o->nup_schedule == 4) {
+            // multiplied at the top of every iteration, the first included
+            // (muca_mag.cpp:131), as the single-context run does
+            const unsigned long long nx = (unsigned long long)((double)c.st.nup * 1.05);
+            const uint32_t cap = o->nup_max ? o->nup_max : (1u << 30);
+            c.st.nup = nx > cap ? (cap > c.st.nup ? cap : c.st.nup) : (uint32_t)nx;
+        }
         c.st.width = 10;
         c.st.total_run = (unsigned long long)c.st.nup * m.nchains;
         c.N = N;
@@ -583,7 +590,7 @@ muca_status muca_batch_run(muca_batch *b, const muca_batch_run_opts *o, muca_bat
     if (o->starting_M == 0 && o->starting_sweeps == 0)
         return bfail(b, MUCA_ERR_BAD_ARG, "starting_M or starting_sweeps must be >= 1");
     if (o->starting_sweeps > 4096) return bfail(b, MUCA_ERR_BAD_ARG, "starting_sweeps=%u (at most 4096)", o->starting_sweeps);
-    if (o->nup_schedule > 3) return bfail(b, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..3)", o->nup_schedule);
+    if (o->nup_schedule > 4) return bfail(b, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..4)", o->nup_schedule);
     const uint32_t K = o->graph_iters ? o->graph_iters : 16u;
     if (K > 4096) return bfail(b, MUCA_ERR_BAD_ARG, "graph_iters=%u (at most 4096)", K);
     BCUDA(b, cudaSetDevice(b->device));

@@ -143,28 +143,35 @@ def ab_test(net, held, opts=RUN_OPTS, device=0, sources=None, graded=False):
         arms["pl"] = [interpolated_weight(L, T, sources, PL_KNOTS) for L, _, T, _, _ in held]
         arms["interp"] = [interpolated_weight(L, T, sources) for L, _, T, _, _ in held]
     rz, sz, wz = converge(held, opts, None, device)
-    runs = {k: converge(held, opts, w, device)[:2] for k, w in arms.items()}
+    runs = {k: converge(held, opts, w, device) for k, w in arms.items()}
+    # the statistical floor of the final weights: the zero weight again with other seeds
+    runs["zero_reseeded"] = converge([(L, nc, T, D, seed + 7919) for L, nc, T, D, seed in held], opts, None,
+                                     device)
+    arms["zero_reseeded"] = [np.zeros_like(w) for w in wz]
     if graded:
         og = dict(opts, reinit_chains=1, graded_init=1)
-        runs["zero_g"] = converge(held, og, None, device)[:2]
+        runs["zero_g"] = converge(held, og, None, device)
         arms["zero_g"] = [np.zeros_like(w) for w in wz]
         for k in [k for k in ("mlp", "interp") if k in arms]:
-            runs[k + "_g"] = converge(held, og, arms[k], device)[:2]
+            runs[k + "_g"] = converge(held, og, arms[k], device)
             arms[k + "_g"] = arms[k]
     rows = []
     for i, (L, nc, T, D, seed) in enumerate(held):
         row = {"L": L, "T": T, "delta": D, "chains": nc, "zero_iters": rz[i].iterations,
                "zero_converged": bool(rz[i].converged), "lnw_range": float(wz[i].max() - wz[i].min())}
-        for k, (r, _) in runs.items():
+        for k, (r, _, wf) in runs.items():
             e = arms[k][i] - wz[i]
+            f = wf[i] - wz[i]
             row[k + "_iters"] = r[i].iterations
             row[k + "_converged"] = bool(r[i].converged)
             row[k + "_lnw_rms_err"] = float(np.sqrt(np.mean((e - e.mean()) ** 2)))
+            # the converged weights against the zero arm's (both shifted to mean zero)
+            row[k + "_final_rms_vs_zero"] = float(np.sqrt(np.mean((f - f.mean()) ** 2)))
         row["surrogate_lnw_rms_err"] = row["mlp_lnw_rms_err"]
         rows.append(row)
     iz = sum(r["zero_iters"] for r in rows)
     out = {"instances": rows, "zero_iters_total": iz, "zero_device_s": sz}
-    for k, (_, s) in runs.items():
+    for k, (_, s, _) in runs.items():
         ik = sum(r[k + "_iters"] for r in rows)
         out[k + "_iters_total"] = ik
         out[k + "_device_s"] = s
@@ -185,6 +192,8 @@ def main(argv=None):
     p.add_argument("--graded", action="store_true", help="also run the arms from graded initial spins")
     p.add_argument("--steps", type=int, default=10000, help="Adam steps per learning-rate stage (3 stages)")
     p.add_argument("--schedule", type=int, default=RUN_OPTS["nup_schedule"])
+    p.add_argument("--ab-schedules", default="",
+                   help="NUPDATES schedules to repeat the A/B with (same network), e.g. 0,4")
     p.add_argument("--device", type=int, default=0)
     a = p.parse_args(argv)
     Ls = [int(v) for v in a.L.split(",")]
@@ -211,7 +220,27 @@ def main(argv=None):
                 for k, (L, T) in enumerate([(L, float(T)) for L in Ls + held_L for T in a.held_T.split(",")])]
         sources = [(train_inst[i][0], train_inst[i][2], W[i]) for i in ok]
         ab = ab_test(net, held, opts, a.device, sources, graded=a.graded)
+        # the A/B under other NUPDATES schedules, both arms alike (the network is the same)
+        ab_sched = {int(sc): ab_test(net, held, dict(opts, nup_schedule=int(sc)), a.device, sources)
+                    for sc in a.ab_schedules.split(",") if sc}
+        if ab_sched:
+            # each start with its own best schedule against the reference's method
+            # (zero weight, schedule 0), from the runs above
+            best = {}
+            for arm in ("zero", "mlp", "pl", "interp"):
+                cand = [(v[arm + "_device_s"], sc, v[arm + "_iters_total"])
+                        for sc, v in list(ab_sched.items()) + [(opts["nup_schedule"], ab)]]
+                t, sc, it = min(cand)
+                best[arm] = {"schedule": sc, "device_s": t, "iters_total": it}
+            if 0 in ab_sched:
+                ref = ab_sched[0]
+                for arm in best:
+                    best[arm]["iters_ratio_vs_reference_method"] = ref["zero_iters_total"] / best[arm]["iters_total"]
+                    best[arm]["time_ratio_vs_reference_method"] = ref["zero_device_s"] / best[arm]["device_s"]
+            ab_sched["best_schedule_per_arm"] = best
     out = {"run_opts": {k: v for k, v in opts.items()}, "training_set": gen, "fit": fit, "ab": ab}
+    if ab_sched:
+        out["ab_schedules"] = ab_sched
     print(json.dumps(out))
     return out
 

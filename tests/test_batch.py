@@ -93,6 +93,20 @@ def test_batch_graded_init_equals_single_simulations(muca):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("sched", [0, 3, 4])
+def test_batch_schedules_equal_single_simulations(muca, sched):
+    kw = dict(nup_schedule=sched, flat_minmean=1, max_iter=25, nup_max=1 << 14)
+    inst = INSTANCES[:3]
+    with muca.Batch(inst) as b:
+        res, _ = b.run(starting_M=1, graph_iters=4, **kw)
+        ws = [b.get_weights(i) for i in range(len(inst))]
+    for i, (L, nc, beta, seed) in enumerate(inst):
+        r, w, _ = _single(muca, L, nc, seed, **kw)
+        assert (res[i].iterations, res[i].total_run) == (r.iterations, r.total_run), i
+        np.testing.assert_array_equal(ws[i], w, err_msg="instance %d" % i)
+
+
+@pytest.mark.gpu
 def test_batch_recursion_doubling_equals_single_simulations(muca):
     kw = dict(rule=muca.UPDATE_RECURSION, nup_schedule=1, flat_minmean=1, max_iter=40)
     inst = INSTANCES[:3]
