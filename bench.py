@@ -388,13 +388,15 @@ def flat_run_metric(local):
     N = L * L
     with m.Engine(L, nchains=nc, device=local) as e:
         res, _ = e.weight_run(starting_M=N, rule=m.UPDATE_TRIVIAL, nup_schedule=1, flat_minmean=1, max_iter=6000,
-                              nup_max=1 << 20, init_scheme=m.INIT_CHAIN_COUNTER, records=1)
+                              nup_max=1 << 20, init_scheme=m.INIT_CHAIN_COUNTER, records=1, graph_iters=32)
     return {"metric": "weight iterations to a flat histogram (min/mean >= 0.5) at L=72", "L": L, "chains": nc,
             "iterations": res.iterations, "converged": bool(res.converged),
             "width_reached_iteration": res.width_reached_iter, "device_s": res.total_kernel_s,
             "wall_s": res.wall_s, "update": "trivial (lnW -= ln H for H > 1, then lnW -= lnW[0])",
             "schedule": "NUPDATES = N, doubling once the width is N (cap 2^20)",
-            "init": "Philox4x32-10, key 2024, counter = chain id"}
+            "init": "Philox4x32-10, key 2024, counter = chain id",
+            "loop": "32 iterations (clear, sweep, update) per CUDA-graph replay; device_s = CUDA events "
+                    "around the replays, wall_s = host clock of the whole run"}
 
 
 def batch_metric(local, iters=32):

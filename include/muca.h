@@ -145,6 +145,10 @@ typedef struct muca_run_opts {
     uint32_t width_start;   /* initial running width (0 = 10, :314); the reference keeps the
                                previous jack's width for jack > 0 */
     uint32_t nup_max;       /* cap of NUPDATES (0: none for schedule 0, 2^30 for the doubling ones) */
+    uint32_t graph_iters;   /* 0: one host round trip per iteration, as the reference loop (records carry
+                               per-iteration kernel times); K > 0: K iterations per CUDA-graph replay
+                               (iterations after the stop do nothing; records carry no kernel times);
+                               ignored by muca_weight_run_stream */
 } muca_run_opts;
 
 typedef struct muca_iter_record {

@@ -77,7 +77,7 @@ class RunOpts(C.Structure):
                 ("hold_until_full", C.c_uint32), ("flat_minmean", C.c_uint32), ("max_iter", C.c_uint32),
                 ("init_scheme", C.c_uint32), ("reinit_chains", C.c_uint32), ("nup_schedule", C.c_uint32),
                 ("min_over_mean", C.c_double), ("d_kl_max", C.c_double), ("width_start", C.c_uint32),
-                ("nup_max", C.c_uint32)]
+                ("nup_max", C.c_uint32), ("graph_iters", C.c_uint32)]
 
 
 class IterRecord(C.Structure):
@@ -365,12 +365,12 @@ class Engine:
 
     def weight_run(self, starting_M=1, jack=0, rule=UPDATE_TRIVIAL, hold_until_full=0, flat_minmean=0,
                    max_iter=0, therm=0, init_scheme=INIT_WEIGHT, reinit_chains=1, nup_schedule=0,
-                   min_over_mean=0.0, d_kl_max=0.0, width_start=0, nup_max=0, records=1000,
+                   min_over_mean=0.0, d_kl_max=0.0, width_start=0, nup_max=0, records=1000, graph_iters=0,
                    raise_on_not_converged=False):
         o = RunOpts(jack=jack, starting_M=starting_M, therm=therm, rule=rule, hold_until_full=hold_until_full,
                     flat_minmean=flat_minmean, max_iter=max_iter, init_scheme=init_scheme,
                     reinit_chains=reinit_chains, nup_schedule=nup_schedule, min_over_mean=min_over_mean,
-                    d_kl_max=d_kl_max, width_start=width_start, nup_max=nup_max)
+                    d_kl_max=d_kl_max, width_start=width_start, nup_max=nup_max, graph_iters=graph_iters)
         res = RunResult()
         recs = (IterRecord * max(records, 1))()
         st = self._lib.muca_weight_run(self._h, C.byref(o), C.byref(res), recs, records)

@@ -682,7 +682,48 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     double tk = 0, tm = 0, nwidth_time = -1;
     uint32_t k_done = 0;
     muca_status rs = MUCA_OK;
-    for (;;) {
+    const bool graph_mode = o->graph_iters > 0 && !cb;
+    if (graph_mode) {
+        // K iterations (clear, sweep, update) captured once and replayed; the
+        // device stops them itself, so one host round trip serves K iterations
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
+        const bool capturing = e == cudaSuccess;
+        for (uint32_t j = 0; j < o->graph_iters && e == cudaSuccess; ++j) {
+            e = launch_run_clear(c->d_hist, (uint32_t)c->hist_len, c->d_ctl, c->stream);
+            if (e == cudaSuccess)
+                e = c->algo == MUCA_ALGO_RANDOM_SITE
+                        ? launch_sweep_random(ra, c->plan.cpb, c->plan.blocks, (int)c->rounds, c->smem_optin, c->stream)
+                        : launch_sweep(c->plan, a, c->stream);
+            if (e == cudaSuccess) e = launch_run_update(c->d_hist, c->d_lnw, c->d_w32, c->d_pacc, c->d_ctl, c->stream,
+                                                        c->N, (int)o->rule);
+        }
+        if (capturing) {
+            const cudaError_t ec = cudaStreamEndCapture(c->stream, &graph);
+            if (e == cudaSuccess) e = ec;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        while (e == cudaSuccess) {
+            e = cudaEventRecord(e0, c->stream);
+            if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&h.st, &c->d_ctl->st, sizeof(IterState), cudaMemcpyDeviceToHost,
+                                                      c->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+            if (e != cudaSuccess) break;
+            float ks = 0;
+            cudaEventElapsedTime(&ks, e0, e1);
+            tk += ks;
+            if (h.st.reach && nwidth_time < 0) nwidth_time = tk;
+            if (h.st.stop) break;
+        }
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) rs = fail(c, MUCA_ERR_CUDA, "weight run (graph): %s", cudaGetErrorString(e));
+        k_done = h.st.converged ? h.st.k + 1u : h.st.k;
+    }
+    while (!graph_mode) {
         // one iteration per host round trip, like the reference loop; the
         // device decides the schedule and convergence
         cudaError_t e = launch_run_clear(c->d_hist, (uint32_t)c->hist_len, c->d_ctl, c->stream);
@@ -738,8 +779,8 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
             recs[i].total_run = r[i].total_run;
             recs[i].d_kl = r[i].d_kl;
             recs[i].min_over_mean = r[i].min_over_mean;
-            recs[i].kernel_ms = kms[i];
-            recs[i].memcpy_ms = mms[i];
+            recs[i].kernel_ms = i < kms.size() ? kms[i] : 0.0;  // none per iteration in graph mode
+            recs[i].memcpy_ms = i < mms.size() ? mms[i] : 0.0;
         }
     }
     if (res) {

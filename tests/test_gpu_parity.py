@@ -518,3 +518,23 @@ def test_iterate_host_equals_separate_calls(muca, rule):
         np.testing.assert_array_equal(wa, wb)
         np.testing.assert_array_equal(ha, hb)
         assert sa == sb
+
+
+@pytest.mark.parametrize("sched,graph_iters", [(0, 7), (1, 16), (4, 3)])
+def test_weight_run_graph_equals_per_iteration(muca, sched, graph_iters):
+    """graph_iters K: K iterations per CUDA-graph replay give the per-iteration
+    loop's run: iterations, NUPDATES totals, weights, histogram, records."""
+    L, nc = 16, 256
+    kw = dict(starting_M=1, nup_schedule=sched, flat_minmean=1, max_iter=300, nup_max=1 << 14, records=400)
+    out = []
+    for g in (0, graph_iters):
+        with muca.Engine(L, nchains=nc) as e:
+            r, recs = e.weight_run(graph_iters=g, **kw)
+            out.append((r, recs, e.get_weights(), e.histogram()))
+    (ra, reca, wa, ha), (rb, recb, wb, hb) = out
+    assert (ra.iterations, ra.converged, ra.total_run, ra.width_reached_iter) == \
+        (rb.iterations, rb.converged, rb.total_run, rb.width_reached_iter)
+    np.testing.assert_array_equal(wa, wb)
+    np.testing.assert_array_equal(ha, hb)
+    assert [(x.k, x.width, x.nupdates, x.total_run, x.d_kl) for x in reca] == \
+        [(x.k, x.width, x.nupdates, x.total_run, x.d_kl) for x in recb]
