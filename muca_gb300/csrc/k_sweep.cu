@@ -98,7 +98,7 @@ enum SlotWord : uint32_t {
     kSlotDE = 4,    // dE as signed bytes, sites 0..3 and 4..7 (two words)
     kSlotF2 = 6,    // -beta dE as floats (8 words)
     kSlotLF = 14,   // __logf(u) (8 words)
-    kSlotP = 22,    // packed draws (8 words): the exact replay and partial windows
+    kSlotP = 22,    // acceptance words for the exact replay, or packed draws of a partial window (8 words)
 };
 static_assert(kSlotP + 8 == kSlotWords, "slot layout");
 

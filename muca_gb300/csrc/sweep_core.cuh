@@ -36,10 +36,11 @@ struct ChainState {
     int E, EJ, M;
 };
 
-// A packed random word per attempt: bits 31..8 are the top 24 bits of the
-// acceptance draw r1 (all that u01fixedpt<float> uses: u = (1|(r1>>8))
-// 2^-24), bit 0 is the direction bit (u01fixedpt<float>(r3) < 0.5 <=>
-// r3 < 2^31, so the bit is r3's top bit, set for s -> s-1).
+// A packed random word per attempt (the step-by-step partial windows take
+// these): bits 31..8 are the top 24 bits of the acceptance draw r1 (all that
+// u01fixedpt<float> uses: u = (1|(r1>>8)) 2^-24), bit 0 is the direction bit
+// (u01fixedpt<float>(r3) < 0.5 <=> r3 < 2^31, so the bit is r3's top bit,
+// set for s -> s-1).
 __device__ __forceinline__ uint32_t pack_draw(uint32_t r1, uint32_t r3) { return (r1 & 0xFFFFFF00u) | (r3 >> 31); }
 
 // One Philox block of the acceptance stream (k1) and one of the direction
@@ -127,7 +128,7 @@ __device__ __forceinline__ void record_window(uint32_t *__restrict__ histS, unsi
 }
 
 // A decoded window: everything its accept/reject scan needs, formed from the
-// lattice words and the packed draws before the scan runs.
+// lattice words and the draws before the scan runs.
 template <int MODE>
 struct WinDec {
     using WT = typename WeightType<MODE>::T;
@@ -136,8 +137,8 @@ struct WinDec {
     int dE[8], dDel[8], dM[8];
     float f2[8];                // -beta dE (an even integer for beta = 2: exact in FP32 and FP64)
     float lf[8];                // __logf(u)
-    uint32_t p[8];              // the packed draws (for the exact replay)
-    const uint32_t *pr;         // or, when set, the draws in shared memory (pr[32 t])
+    uint32_t p[8];              // the acceptance words (for the exact replay; bits 31..9 used)
+    const uint32_t *pr;         // or, when set, those words in shared memory (pr[32 t])
 };
 
 // Decodes the SLOTS same-parity sites (half 0: even, 1: odd) of word q of
@@ -558,8 +559,9 @@ __device__ __forceinline__ bool launch_params(const SweepArgs &a, uint32_t &iter
 
 
 // The windowed sweep of chain block `blk` (cpb chains, lanes >= cpb are
-// padding): every lane draws its own Philox numbers one window ahead (`next`
-// holds the packed draws of the next two groups, counters cc-1, cc).  Ends
+// padding): every lane draws its own Philox numbers one window ahead (n1/n3
+// hold the acceptance and direction words of the next two groups, counters
+// cc-1, cc).  Ends
 // with the block synchronised and, with HS, the shared histogram drained.
 template <int MODE, int R, bool LAT_SMEM, bool HS = true, bool BT = false>
 __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned char *smem, uint32_t cpb, uint32_t blk,
