@@ -49,6 +49,11 @@ def test_null_arguments(libmuca):
     assert libmuca.muca_create(None, None) == 1
     assert libmuca.muca_destroy(None) == 0
     assert libmuca.muca_get_info(None, None) == 1
+    # no context: every per-context call is a BAD_ARG, never a crash
+    assert libmuca.muca_iterate_host(None, None, 0, 100, 1000, 16, 16, 0, None, None, None) == 1
+    assert libmuca.muca_sweep(None, 0, 100, 1000, 16, 16) == 1
+    assert libmuca.muca_update_weights(None, 0, None) == 1
+    assert libmuca.muca_init_chains(None, 5, 0) == 1
 
 
 def test_no_gpu_fails_loudly(libmuca):

@@ -538,3 +538,22 @@ def test_weight_run_graph_equals_per_iteration(muca, sched, graph_iters):
     np.testing.assert_array_equal(ha, hb)
     assert [(x.k, x.width, x.nupdates, x.total_run, x.d_kl) for x in reca] == \
         [(x.k, x.width, x.nupdates, x.total_run, x.d_kl) for x in recb]
+
+
+def test_iterate_host_rejects_bad_calls(muca):
+    L = 8
+    N = L * L
+    with muca.Engine(L, nchains=64) as e:
+        w = np.zeros(N + 1)
+        with pytest.raises(muca.MucaError, match="rule"):
+            e.iterate_host(w, 0, 100, 1000, N, N, rule=7)
+        w[3] = np.nan
+        with pytest.raises(muca.MucaError, match="finite"):
+            e.iterate_host(w, 0, 100, 1000, N, N)
+        with pytest.raises(ValueError):
+            e.iterate_host(np.zeros(N), 0, 100, 1000, N, N)
+        # NULL in and out: the device weights are kept, nothing is copied
+        e.iterate_host(None, 0, 100, 1000, N, N)
+    with muca.Engine(L, nchains=64, mode=muca.MODE_PRODUCE) as e:
+        with pytest.raises(muca.MucaError, match="weight-mode"):
+            e.iterate_host(None, 0, 100, 1000, N, N)
