@@ -18,6 +18,8 @@ namespace muca {
 
 constexpr int kUpdThreads = 1024;
 
+// Reduction over a block of whole warps; lanes beyond the number of warps
+// enter the second stage with the operation's identity.
 template <typename T, typename Op>
 __device__ T block_reduce(T v, Op op, T *sh)
 {
@@ -27,7 +29,7 @@ __device__ T block_reduce(T v, Op op, T *sh)
     if (lane == 0) sh[wid] = v;
     __syncthreads();
     if (wid == 0) {
-        v = lane < nw ? sh[lane] : sh[0];
+        v = lane < nw ? sh[lane] : Op::id();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
         if (lane == 0) sh[0] = v;
@@ -38,11 +40,26 @@ __device__ T block_reduce(T v, Op op, T *sh)
     return r;
 }
 
-struct MinI { __device__ int operator()(int a, int b) const { return a < b ? a : b; } };
-struct MaxI { __device__ int operator()(int a, int b) const { return a > b ? a : b; } };
-struct AddU { __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return a + b; } };
-struct MinU { __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return a < b ? a : b; } };
-struct AddD { __device__ double operator()(double a, double b) const { return a + b; } };
+struct MinI {
+    __device__ int operator()(int a, int b) const { return a < b ? a : b; }
+    __device__ static int id() { return 0x7FFFFFFF; }
+};
+struct MaxI {
+    __device__ int operator()(int a, int b) const { return a > b ? a : b; }
+    __device__ static int id() { return -0x7FFFFFFF - 1; }
+};
+struct AddU {
+    __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return a + b; }
+    __device__ static unsigned long long id() { return 0ull; }
+};
+struct MinU {
+    __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return a < b ? a : b; }
+    __device__ static unsigned long long id() { return ~0ull; }
+};
+struct AddD {
+    __device__ double operator()(double a, double b) const { return a + b; }
+    __device__ static double id() { return 0.0; }
+};
 
 // Statistics of hist[0..N], then (if the update is due) the weight update.
 // ctl == nullptr: standalone call, update iff rule >= 0.
@@ -71,6 +88,57 @@ __host__ __device__ __forceinline__ uint32_t next_nupdates(uint32_t nup, bool fu
     }
     if (cap != 0 && nx > cap) nx = cap > nup ? cap : nup;
     return (uint32_t)nx;
+}
+
+// The statistics' consumers, one thread: the stats record, and in a
+// device-driven run the running width, convergence, record and NUPDATES of
+// the next iteration (muca_delta_multigpu.cu:431-447,464-466).  Returns
+// whether the weights are to be updated.
+__device__ __forceinline__ int bookkeep(int start, int end, unsigned long long vis, unsigned long long ev,
+                                        unsigned long long mn, double kl, uint32_t N, int rule,
+                                        HistStatsDev *__restrict__ stats, RunCtl *__restrict__ ctl)
+{
+    const double mean = __ddiv_rn((double)ev, (double)(N + 1));
+    const double mom = mean > 0 ? __ddiv_rn((double)mn, mean) : 0.0;
+    if (stats) {
+        stats->start = start;
+        stats->end = end;
+        stats->width = (uint32_t)(end - start);
+        stats->visited = (uint32_t)vis;
+        stats->events = ev;
+        stats->min_count = mn;
+        stats->d_kl = kl;
+        stats->min_over_mean = mom;
+    }
+    int upd = rule >= 0;
+    if (ctl) {
+        IterState &st = ctl->st;
+        const uint32_t wt = (uint32_t)(end - start);
+        st.width_temp = wt;
+        if (wt > st.width) st.width = wt;
+        if (st.width == N && !st.reach) { st.reach = 1; st.reach_k = st.k; st.nwidth_step = st.total_run; }
+        const bool conv = ctl->flat_minmean ? (mom >= ctl->mom_thr) : (st.width == N && kl < ctl->dkl_max);
+        const uint32_t ri = ctl->rec_ring ? (ctl->rec_cap ? st.k % ctl->rec_cap : 0u) : st.k;
+        if (ri < ctl->rec_cap && ctl->recs) {
+            IterRecordDev &r = ctl->recs[ri];
+            r.k = st.k; r.width_temp = wt; r.width = st.width; r.nupdates = st.nup;
+            r.total_run = st.total_run; r.d_kl = kl; r.min_over_mean = mom;
+        }
+        upd = !conv && (!ctl->hold || st.width == N);
+        if (conv) {
+            st.converged = 1;
+            st.stop = 1;
+        } else {
+            st.k += 1;
+            if (st.k >= ctl->max_iter) {
+                st.stop = 1;
+            } else {
+                st.nup = next_nupdates(st.nup, st.width == N, mom >= 0.05, ctl->sched, ctl->nup_max);
+                st.total_run += (unsigned long long)st.nup * ctl->nchains_total;
+            }
+        }
+    }
+    return upd;
 }
 
 // `dyn`: dynamic shared memory of update_smem(N, rule) bytes.
@@ -118,50 +186,7 @@ __device__ __forceinline__ void weight_update_body(const unsigned long long *__r
         }
     }
     kl = block_reduce(kl, AddD(), shd);
-    const double mean = __ddiv_rn((double)ev, (double)(N + 1));
-    const double mom = mean > 0 ? __ddiv_rn((double)mn, mean) : 0.0;
-    if (tid == 0) {
-        if (stats) {
-            stats->start = start;
-            stats->end = end;
-            stats->width = (uint32_t)(end - start);
-            stats->visited = (uint32_t)vis;
-            stats->events = ev;
-            stats->min_count = mn;
-            stats->d_kl = kl;
-            stats->min_over_mean = mom;
-        }
-        int upd = rule >= 0;
-        if (ctl) {
-            // muca_delta_multigpu.cu:431-447,464-466
-            IterState &st = ctl->st;
-            const uint32_t wt = (uint32_t)(end - start);
-            st.width_temp = wt;
-            if (wt > st.width) st.width = wt;
-            if (st.width == N && !st.reach) { st.reach = 1; st.reach_k = st.k; st.nwidth_step = st.total_run; }
-            const bool conv = ctl->flat_minmean ? (mom >= ctl->mom_thr) : (st.width == N && kl < ctl->dkl_max);
-            const uint32_t ri = ctl->rec_ring ? (ctl->rec_cap ? st.k % ctl->rec_cap : 0u) : st.k;
-            if (ri < ctl->rec_cap && ctl->recs) {
-                IterRecordDev &r = ctl->recs[ri];
-                r.k = st.k; r.width_temp = wt; r.width = st.width; r.nupdates = st.nup;
-                r.total_run = st.total_run; r.d_kl = kl; r.min_over_mean = mom;
-            }
-            upd = !conv && (!ctl->hold || st.width == N);
-            if (conv) {
-                st.converged = 1;
-                st.stop = 1;
-            } else {
-                st.k += 1;
-                if (st.k >= ctl->max_iter) {
-                    st.stop = 1;
-                } else {
-                    st.nup = next_nupdates(st.nup, st.width == N, mom >= 0.05, ctl->sched, ctl->nup_max);
-                    st.total_run += (unsigned long long)st.nup * ctl->nchains_total;
-                }
-            }
-        }
-        do_update = upd;
-    }
+    if (tid == 0) do_update = bookkeep(start, end, vis, ev, mn, kl, N, rule, stats, ctl);
     __syncthreads();
     if (!do_update) return;
 
@@ -231,6 +256,151 @@ __global__ void __launch_bounds__(kUpdThreads) k_weight_update(const unsigned lo
     weight_update_body(hist, N, lnw, w32, p_acc, rule, stats, ctl, dyn);
 }
 
+// ---- the same statistics and update over kUpdBlocks blocks ---------------
+// The divergence terms and the ln H of the update are FP64 per bin, and FP64
+// issues slowly on this GPU: one block leaves all of them to one SM (ncu:
+// 67 % of that SM's FP64 pipe, 28 us at L=72).  Here pass 1 forms the integer
+// statistics per block; pass 2 the divergence terms per block, after every
+// block has summed the partial event and visited counts in block order; the
+// last block of pass 2 sums all partials in block order, keeps the books as
+// the one-block update does (bookkeep) and decides the update; pass 3
+// applies it.  Integer statistics and the updated weights equal the one-block
+// update's; the divergence sum runs in another order.
+constexpr int kUpdMultiThreads = 256;
+
+__global__ void __launch_bounds__(kUpdMultiThreads) k_upd_stats(const unsigned long long *__restrict__ hist,
+                                                                uint32_t N, const RunCtl *__restrict__ ctl,
+                                                                UpdScratch *__restrict__ sc)
+{
+    __shared__ int shi[32];
+    __shared__ unsigned long long shu[32];
+    if (ctl && ctl->st.stop) return;
+    int lo = (int)N + 1, hi = -1;
+    unsigned long long vis = 0, ev = 0, mn = ~0ull;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= N; i += gridDim.x * blockDim.x) {
+        const unsigned long long h = hist[i];
+        if (h > 1) { lo = min(lo, (int)i); hi = max(hi, (int)i); }
+        if (h > 0) { ++vis; ev += h; }
+        mn = h < mn ? h : mn;
+    }
+    lo = block_reduce(lo, MinI(), shi);
+    hi = block_reduce(hi, MaxI(), shi);
+    vis = block_reduce(vis, AddU(), shu);
+    ev = block_reduce(ev, AddU(), shu);
+    mn = block_reduce(mn, MinU(), shu);
+    if (threadIdx.x == 0) {
+        UpdPart &p = sc->part[blockIdx.x];
+        p.lo = lo; p.hi = hi; p.vis = vis; p.ev = ev; p.mn = mn;
+    }
+}
+
+__global__ void __launch_bounds__(kUpdMultiThreads) k_upd_kl(const unsigned long long *__restrict__ hist, uint32_t N,
+                                                             const double *__restrict__ lnw, int rule,
+                                                             HistStatsDev *__restrict__ stats,
+                                                             RunCtl *__restrict__ ctl, UpdScratch *__restrict__ sc)
+{
+    __shared__ double shd[32];
+    __shared__ unsigned long long s_ev, s_vis;
+    __shared__ int s_last;
+    if (ctl && ctl->st.stop) {
+        // an iteration after the stop: no update either
+        if (blockIdx.x == 0 && threadIdx.x == 0) sc->upd = 0;
+        return;
+    }
+    if (threadIdx.x < 32) {
+        // the partial counts, two per lane, then a warp sum (fixed order)
+        unsigned long long e = 0, v = 0;
+        for (uint32_t b = threadIdx.x; b < gridDim.x; b += 32) { e += sc->part[b].ev; v += sc->part[b].vis; }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            e += __shfl_xor_sync(0xffffffffu, e, o);
+            v += __shfl_xor_sync(0xffffffffu, v, o);
+        }
+        if (threadIdx.x == 0) {
+            s_ev = e;
+            s_vis = v;
+        }
+    }
+    __syncthreads();
+    // sum over H>0 of P ln(P/Q), P = H/events, Q = 1/visited (as the one-block update)
+    const double num_event = (double)s_ev, Q = __ddiv_rn(1.0, (double)s_vis);
+    double kl = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= N; i += gridDim.x * blockDim.x) {
+        const unsigned long long h = hist[i];
+        if (h > 0) {
+            const double P = __ddiv_rn((double)h, num_event);
+            kl = __dadd_rn(kl, __dmul_rn(P, log(__ddiv_rn(P, Q))));
+        }
+    }
+    kl = block_reduce(kl, AddD(), shd);
+    if (threadIdx.x == 0) {
+        sc->part[blockIdx.x].kl = kl;
+        __threadfence();
+        s_last = atomicAdd(&sc->done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last || threadIdx.x >= 32) return;
+    __threadfence();
+    // all partials, two per lane, then warp reductions (fixed order)
+    int lo = (int)N + 1, hi = -1;
+    unsigned long long vis = 0, ev = 0, mn = ~0ull;
+    double klt = 0.0;
+    for (uint32_t b = threadIdx.x; b < gridDim.x; b += 32) {
+        const UpdPart &p = sc->part[b];
+        lo = min(lo, p.lo);
+        hi = max(hi, p.hi);
+        vis += p.vis;
+        ev += p.ev;
+        mn = p.mn < mn ? p.mn : mn;
+        klt = __dadd_rn(klt, __ldcg(&p.kl));  // written by other blocks of this launch
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        vis += __shfl_xor_sync(0xffffffffu, vis, o);
+        ev += __shfl_xor_sync(0xffffffffu, ev, o);
+        const unsigned long long m2 = __shfl_xor_sync(0xffffffffu, mn, o);
+        mn = m2 < mn ? m2 : mn;
+        klt = __dadd_rn(klt, __shfl_xor_sync(0xffffffffu, klt, o));
+    }
+    if (threadIdx.x != 0) return;
+    int start = lo, end = hi < 0 ? 0 : hi;
+    if (start > end) { start = 0; end = 0; }
+    sc->upd = bookkeep(start, end, vis, ev, mn, klt, N, rule, stats, ctl);
+    // lnW[0] after its ln H subtraction (:469), from the weights before any write
+    const unsigned long long h0 = hist[0], thr = rule == 0 ? 1ull : 0ull;
+    sc->tmp = h0 > thr ? __dsub_rn(lnw[0], log((double)h0)) : lnw[0];
+    sc->done = 0;
+}
+
+__global__ void __launch_bounds__(kUpdMultiThreads) k_upd_apply(const unsigned long long *__restrict__ hist,
+                                                                uint32_t N, double *__restrict__ lnw,
+                                                                float *__restrict__ w32, int rule,
+                                                                const UpdScratch *__restrict__ sc)
+{
+    if (!sc->upd) return;
+    const unsigned long long thr = rule == 0 ? 1ull : 0ull;
+    const double tmp = sc->tmp;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= N; i += gridDim.x * blockDim.x) {
+        const unsigned long long h = hist[i];
+        double v = lnw[i];
+        if (h > thr) v = __dsub_rn(v, log((double)h));
+        if (rule == 0 || h > 0) v = __dsub_rn(v, tmp);
+        lnw[i] = v;
+        w32[i] = (float)v;
+    }
+}
+
+static cudaError_t launch_update_multi(const unsigned long long *hist, uint32_t N, double *lnw, float *w32,
+                                       int rule, HistStatsDev *stats, RunCtl *ctl, UpdScratch *sc, cudaStream_t s)
+{
+    k_upd_stats<<<kUpdBlocks, kUpdMultiThreads, 0, s>>>(hist, N, ctl, sc);
+    k_upd_kl<<<kUpdBlocks, kUpdMultiThreads, 0, s>>>(hist, N, lnw, rule, stats, ctl, sc);
+    if (rule >= 0) k_upd_apply<<<kUpdBlocks, kUpdMultiThreads, 0, s>>>(hist, N, lnw, w32, rule, sc);
+    return cudaGetLastError();
+}
+
 // One iteration's tail for every instance of a batch (block i = instance i),
 // then the count of instances that are still running.
 __global__ void __launch_bounds__(kUpdThreads) k_batch_update(const BatchInst *__restrict__ insts,
@@ -264,8 +434,9 @@ static cudaError_t prep_update(uint32_t N, int rule)
 }
 
 cudaError_t launch_weight_update(const unsigned long long *hist, uint32_t N, double *lnw, float *w32, double *p_acc,
-                                 int rule, HistStatsDev *stats, cudaStream_t s)
+                                 int rule, HistStatsDev *stats, cudaStream_t s, UpdScratch *sc)
 {
+    if (sc && rule != 2) return launch_update_multi(hist, N, lnw, w32, rule, stats, nullptr, sc, s);
     cudaError_t e = prep_update(N, rule);
     if (e != cudaSuccess) return e;
     k_weight_update<<<1, kUpdThreads, update_smem(N, rule), s>>>(hist, N, lnw, w32, p_acc, rule, stats, nullptr);
@@ -273,8 +444,9 @@ cudaError_t launch_weight_update(const unsigned long long *hist, uint32_t N, dou
 }
 
 cudaError_t launch_run_update(const unsigned long long *hist, double *lnw, float *w32, double *p_acc, RunCtl *ctl,
-                              cudaStream_t s, uint32_t N, int rule)
+                              cudaStream_t s, uint32_t N, int rule, UpdScratch *sc)
 {
+    if (sc && rule != 2) return launch_update_multi(hist, N, lnw, w32, rule, nullptr, ctl, sc, s);
     cudaError_t e = prep_update(N, rule);
     if (e != cudaSuccess) return e;
     k_weight_update<<<1, kUpdThreads, update_smem(N, rule), s>>>(hist, N, lnw, w32, p_acc, rule, nullptr, ctl);

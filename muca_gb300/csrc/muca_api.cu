@@ -35,6 +35,7 @@ struct muca_ctx {
     unsigned long long *d_hist = nullptr;
     uint32_t *d_index = nullptr, *d_naver = nullptr;
     HistStatsDev *d_stats = nullptr, *h_stats = nullptr;
+    UpdScratch *d_upd = nullptr;  // the multi-block weight update
     RunCtl *d_ctl = nullptr, *h_ctl = nullptr;
     IterRecordDev *d_recs = nullptr;
     size_t recs_cap = 0;
@@ -84,7 +85,7 @@ void free_all(muca_ctx *c)
 {
     void *dp[] = {c->d_lat, c->d_ej, c->d_edel, c->d_mag, c->d_lnw, c->d_lnw_obs, c->d_pacc, c->d_w32, c->d_hist,
                   c->d_index, c->d_naver, c->d_stats, c->d_ctl, c->d_recs, c->d_obs_part, c->d_obs_out,
-                  c->d_jk, c->d_tmp, c->d_bad, c->d_err, c->d_logf_tab};
+                  c->d_jk, c->d_tmp, c->d_bad, c->d_err, c->d_logf_tab, c->d_upd};
     for (void *p : dp)
         if (p) cudaFree(p);
     void *hp[] = {c->h_stats, c->h_ctl, c->h_obs_out, c->h_bad, c->h_err};
@@ -299,6 +300,8 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
     CREATE_TRY(dmalloc(c, &c->d_w32, (size_t)N + 1));
     CREATE_TRY(dmalloc(c, &c->d_hist, c->hist_len));
     CREATE_TRY(dmalloc(c, &c->d_stats, 1));
+    CREATE_TRY(dmalloc(c, &c->d_upd, 1));
+    CREATE_TRY(cudaMemsetAsync(c->d_upd, 0, sizeof(UpdScratch), c->stream));
     CREATE_TRY(dmalloc(c, &c->d_ctl, 1));
     CREATE_TRY(dmalloc(c, &c->d_bad, 1));
     CREATE_TRY(dmalloc(c, &c->d_err, 1));
@@ -563,7 +566,7 @@ static muca_status update_impl(muca_ctx *c, int rule, muca_hist_stats *st)
     if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
     if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "weight statistics need a weight-mode context");
     CUDA_TRY(c, cudaSetDevice(c->device));
-    CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, rule, c->d_stats, c->stream));
+    CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, rule, c->d_stats, c->stream, c->d_upd));
     if (!st) return MUCA_OK;  // enqueue only
     CUDA_TRY(c, cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(HistStatsDev), cudaMemcpyDeviceToHost, c->stream));
     if (muca_status e = check_err(c)) return e;
@@ -602,7 +605,8 @@ muca_status muca_iterate_host(muca_ctx *c, const double *lnw_in, uint32_t iter, 
         CUDA_TRY(c, launch_weights_to_f32(c->d_lnw, c->d_w32, (uint32_t)n, c->stream));
     }
     if (muca_status e = do_sweep(c, iter, seed_base, seed_dev_mul, therm, nup, true)) return e;
-    CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, (int)rule, c->d_stats, c->stream));
+    CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, (int)rule, c->d_stats, c->stream,
+                                     c->d_upd));
     if (st) CUDA_TRY(c, cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(HistStatsDev), cudaMemcpyDeviceToHost, c->stream));
     if (lnw_out) CUDA_TRY(c, cudaMemcpyAsync(lnw_out, c->d_lnw, n * 8, cudaMemcpyDeviceToHost, c->stream));
     if (hist_out) CUDA_TRY(c, cudaMemcpyAsync(hist_out, c->d_hist, n * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -697,7 +701,7 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
                         ? launch_sweep_random(ra, c->plan.cpb, c->plan.blocks, (int)c->rounds, c->smem_optin, c->stream)
                         : launch_sweep(c->plan, a, c->stream);
             if (e == cudaSuccess) e = launch_run_update(c->d_hist, c->d_lnw, c->d_w32, c->d_pacc, c->d_ctl, c->stream,
-                                                        c->N, (int)o->rule);
+                                                        c->N, (int)o->rule, c->d_upd);
         }
         if (capturing) {
             const cudaError_t ec = cudaStreamEndCapture(c->stream, &graph);
@@ -734,7 +738,7 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
                     : launch_sweep(c->plan, a, c->stream);
         if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
         if (e == cudaSuccess) e = launch_run_update(c->d_hist, c->d_lnw, c->d_w32, c->d_pacc, c->d_ctl, c->stream,
-                                                    c->N, (int)o->rule);
+                                                        c->N, (int)o->rule, c->d_upd);
         if (e == cudaSuccess) e = cudaEventRecord(m0, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(&h.st, &c->d_ctl->st, sizeof(IterState), cudaMemcpyDeviceToHost, c->stream);
         if (e == cudaSuccess) e = cudaEventRecord(m1, c->stream);

@@ -115,10 +115,28 @@ struct HistStatsDev {
     unsigned long long events, min_count;
     double d_kl, min_over_mean;
 };
+// Scratch of the multi-block weight update of one context: per-block
+// partial statistics, the count of finished blocks, and the decision the
+// last block takes for the update pass.
+constexpr uint32_t kUpdBlocks = 64;
+struct UpdPart {
+    int lo, hi;
+    unsigned long long vis, ev, mn;
+    double kl;
+};
+struct UpdScratch {
+    UpdPart part[kUpdBlocks];
+    unsigned int done;
+    int upd;
+    double tmp;
+};
 // stats of hist[0..N]; if rule >= 0 also updates lnw (FP64) / w32 (FP32 shadow)
-// (rule: 0 trivial, 1 trivial-cpu, 2 recursion with p_acc).
+// (rule: 0 trivial, 1 trivial-cpu, 2 recursion with p_acc).  With `sc`
+// (zero-initialised once) rules -1, 0 and 1 spread their FP64 work over
+// kUpdBlocks blocks; the recursion always runs in one block.
 cudaError_t launch_weight_update(const unsigned long long *hist, uint32_t N, double *lnw, float *w32,
-                                 double *p_acc, int rule, HistStatsDev *stats, cudaStream_t s);
+                                 double *p_acc, int rule, HistStatsDev *stats, cudaStream_t s,
+                                 UpdScratch *sc = nullptr);
 
 // Device-resident state of a weight-estimation run (the loop of
 // muca_delta_multigpu.cu:374-477).  The first three words are what the
@@ -187,7 +205,7 @@ cudaError_t launch_batch_update(const BatchInst *insts, uint32_t n_inst, uint32_
 // One iteration's tail: statistics, width/convergence bookkeeping, weight
 // update, schedule of the next NUPDATES; a no-op once st.stop is set.
 cudaError_t launch_run_update(const unsigned long long *hist, double *lnw, float *w32, double *p_acc,
-                              RunCtl *ctl, cudaStream_t s, uint32_t N, int rule);
+                              RunCtl *ctl, cudaStream_t s, uint32_t N, int rule, UpdScratch *sc = nullptr);
 // Clears the weight histogram unless the run has stopped.
 cudaError_t launch_run_clear(unsigned long long *hist, uint32_t n, const RunCtl *ctl, cudaStream_t s);
 cudaError_t launch_weights_to_f32(const double *lnw, float *w32, uint32_t n, cudaStream_t s);
