@@ -352,7 +352,7 @@ def ours_arm(args, ws, rank, local):
                              "frac": PHILOX_BLOCKS_PER_ATTEMPT * att_rate / philox_peak,
                              "peak_source": "measured (muca_philox_peak on this GPU)"},
             "roofline_issue": issue_roofline(prof, sweep_avg, clk, eng.info.sms),
-            "sweep_ms": 1e3 * sweep_avg, "gpu_launches": 2 * args.steps,
+            "sweep_ms": 1e3 * sweep_avg, "gpu_launches": 4 * args.steps,  # per step: the sweep and the three passes of the update
             "clocks": clk, "wall_s_timed_region": t_wall,
         }
     eng.close()
