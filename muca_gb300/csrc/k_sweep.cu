@@ -439,6 +439,13 @@ cudaError_t device_log_eps(int device, cudaStream_t s, double *eps)
 SweepPlan plan_sweep(int mode, int rounds, uint32_t L, uint32_t nchains, size_t smem_optin, int sms, int kernel)
 {
     SweepPlan p{};
+    if (kernel < 0 && mode == kModeProduce && L % 8 == 0 && L >= 8) {
+        // production with the lattice in global memory (large L): the
+        // warp-specialised kernel's second instruction stream pays there
+        // (bit-identical, +1.5-2 % at L=128); elsewhere the windowed kernel
+        const SweepPlan w = plan_sweep(mode, rounds, L, nchains, smem_optin, sms, kKernelWindowed);
+        return w.lat_smem ? w : plan_sweep(mode, rounds, L, nchains, smem_optin, sms, kKernelSpecialized);
+    }
     p.mode = mode;
     p.rounds = rounds;
     p.fast = (L % 8 == 0) && L >= 8;
