@@ -227,3 +227,66 @@ def test_produce_gpu_reuse_first_point_is_the_plain_run(exes, tmp_path):
         outs.append((d / name).read_text().splitlines())
     assert outs[0][0] == outs[1][0]
     assert outs[0][1:] != outs[1][1:]
+
+
+def _weight_oracle(orc, L, NW, lnw0, recursive, max_iter):
+    o = orc.WeightOpts(L=L, nchains=NW, jack=0, gpu=0, starting_M=1, recursive=recursive, hold_until_full=0,
+                       flat_minmean=0, max_iter=max_iter, rounds=7, nthreads=8, width_start=0)
+    N = L * L
+    lnw = np.array(lnw0, np.float64)
+    pacc = np.zeros(N + 1)
+    rec = np.zeros(5 * max_iter)
+    conv = ctypes.c_int()
+    lat = orc.init_lattice(L, NW, orc.scheme_weight(0, 0)).reshape(-1).copy()
+    ej, ed, _ = orc.energies(L, lat.reshape(NW, N))
+    it = orc.lib().orc_weight_run(ctypes.byref(o), lat, ej, ed, lnw, pacc, rec, max_iter, ctypes.byref(conv))
+    return it, bool(conv.value), rec.reshape(-1, 5)[:it], lnw
+
+
+def _check_log(rows, it, rec):
+    assert len(rows) == it
+    for k, row in enumerate(rows):
+        assert int(row[0]) == k
+        assert int(row[1]) == int(rec[k, 0])
+        np.testing.assert_allclose(float(row[2]), rec[k, 1], rtol=2e-5)
+        assert int(row[6]) == int(rec[k, 2]) and int(row[7]) == int(rec[k, 3])
+
+
+@pytest.mark.gpu
+def test_multigpu_weight_continuing_matches_oracle(exes, orc, tmp_path):
+    """continuing=1: the weights start from initweight_L128_T050.txt (one value
+    per line, muca_delta_multigpu.cu:223-235), the files carry the
+    extrapolated-init names."""
+    L, NW = 4, 256
+    N = L * L
+    d = tmp_path / "fss" / ("L%d" % L)
+    d.mkdir(parents=True)
+    w0 = -1.7 * np.arange(N + 1) + 0.05 * np.arange(N + 1) ** 2
+    (d / "initweight_L128_T050.txt").write_text("".join("%.17g\n" % v for v in w0))
+    r = subprocess.run([exes[0], str(L), "0", "0", "1", "1", "0", "1", "--chains=%d" % NW, "--max-iter=3000"],
+                       capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stderr
+    it, conv, rec, lnw = _weight_oracle(orc, L, NW, w0, 0, 3000)
+    rows = [ln.split() for ln in (d / ("shortiter_gpu1_T050c%d_M1_therm1N_Jack0_extrapolated1.txt" % NW))
+            .read_text().splitlines()[1:]]
+    _check_log(rows, it, rec)
+    assert conv
+    w = np.loadtxt(d / ("weight_gpu1_T050c%d_M1_therm1N_JACK0_DKL1e-4_fromextrapolatedinit1.txt" % NW))
+    np.testing.assert_allclose(w[:, 1], lnw, rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.gpu
+def test_multigpu_weight_recursion_matches_oracle(exes, orc, tmp_path):
+    """recursive_update=1: weight_recursion after every iteration (the
+    reference parses the flag but never calls it); the iteration log follows
+    the oracle's recursion step for step."""
+    L, NW, K = 4, 256, 60
+    r = subprocess.run([exes[0], str(L), "0", "0", "1", "1", "1", "0", "--chains=%d" % NW, "--max-iter=%d" % K],
+                       capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stderr
+    N = L * L
+    it, conv, rec, _ = _weight_oracle(orc, L, NW, np.zeros(N + 1), 1, K)
+    d = tmp_path / "fss" / ("L%d" % L)
+    rows = [ln.split() for ln in (d / ("shortiter_gpu1_T050c%d_M1_therm1N_Jack0_iterupdate1.01_rand.txt" % NW))
+            .read_text().splitlines()[1:]]
+    _check_log(rows, it, rec)
