@@ -263,7 +263,7 @@ muca_status muca_compute_observables(muca_ctx *ctx, double beta, double delta, m
  * device buffers owned by the caller; no context.  The call allocates
  * nothing: for callers that must not see a device allocation (a scheduler
  * owning HBM through its own pool and budget; a process that only reweights
- * histograms it holds).  Its scratch is a fixed device array of 608 x 4
+ * histograms it holds).  Its scratch is a fixed device array of 304 x 4
  * doubles inside the library, whose address is looked up on the first call
  * per device; make that first call before any stream capture, since it may
  * load the module.  Nothing needs to start at zero.  Two calls in flight at
