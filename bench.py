@@ -423,7 +423,7 @@ def batch_metric(local, iters=32):
             "graph": "%d iterations (clear, persistent sweep, update) per CUDA graph" % iters}
 
 
-def production_metric(local, L=128, with_ref=True):
+def production_metric(local, L=128, with_ref=True, kernel=0):
     """Production at L=128, 16384 chains (the L=128 configuration's shapes,
     with the sweep counts scaled down): FP64 weights, 2D (E_Delta, M) u64
     histogram of 134 M bins; then the reweighting of that histogram."""
@@ -433,7 +433,7 @@ def production_metric(local, L=128, with_ref=True):
     nc = 16384
     N = L * L
     stream = torch.cuda.Stream()
-    with m.Engine(L, nchains=nc, device=local, mode=m.MODE_PRODUCE, stream=stream.cuda_stream) as e:
+    with m.Engine(L, nchains=nc, device=local, mode=m.MODE_PRODUCE, stream=stream.cuda_stream, kernel=kernel) as e:
         e.init_chains(m.INIT_PRODUCE, 0)
         e.set_weights(np.zeros(N + 1))
         e.sweep(0, 100, 1000, N, 0)  # one thermalisation sweep
@@ -518,7 +518,7 @@ def main():
         from muca_gb300 import build as b
         b.build()
         fn = {"flat_run": flat_run_metric, "batch": batch_metric,
-              "production": lambda d: production_metric(d, args.production_L, with_ref=False)}[args.only]
+              "production": lambda d: production_metric(d, args.production_L, with_ref=False, kernel=args.kernel)}[args.only]
         print(json.dumps(fn(local)))
         return 0
     return ours_arm(args, ws, rank, local)

@@ -233,7 +233,7 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
         // is the reference's.
         const float2 *T = reinterpret_cast<const float2 *>(wS);
         const ChainState s0 = st;
-        const float epsf = (float)eps;
+        const float band = tol + (float)eps;
         float2 tE = T[st.E];
         float2 tN = T[st.E + d.dDel[0]];
         uint32_t accm = 0;
@@ -244,16 +244,15 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
             const int dd = d.dDel[t];
             const float dl = dd == 0 ? 0.0f : (dd < 0 ? tE.x : tE.y);
             const float fast = __fadd_rn(d.f2[t], dl);
-            const float l = d.lf[t];
-            const bool acc = store && ((fast >= 0.0f) || (l < fast));
-            // With a zero difference (dDel = 0, or equal neighbouring weights)
-            // fast is f2 itself and the FP64 diff is f2 + e with
-            // |e| <= 2^-53 (|w| + 16): the same sign, and a zero f2 leaves
-            // diff >= 0 or a negative diff that every logf(u) < 0 clears --
-            // accepted either way.  Only a nonzero difference can put the
-            // sign in doubt; the comparison with log(u) is in doubt when
-            // __logf(u) lies within tol + eps of fast.
-            near |= ((dl != 0.0f) && (fabsf(fast) <= tol)) || ((fast < 0.0f) && (fabsf(l - fast) <= tol + epsf));
+            // logf(u) < 0 for every u = (1|(r>>8)) 2^-24 <= 1 - 2^-24, so the
+            // reference's  diff >= 0 || logf(u) < diff  is  logf(u) < diff.
+            // With |fast - diff| <= tol (any dDel, a zero difference
+            // included) and |__logf(u) - logf(u)| <= eps, the sign of
+            // g = __logf(u) - fast is that of logf(u) - diff whenever
+            // |g| > tol + eps; otherwise the window is replayed.
+            const float g = __fsub_rn(d.lf[t], fast);
+            const bool acc = store && (g < 0.0f);
+            near |= fabsf(g) <= band;
             if (acc) {
                 st.E += dd;
                 st.EJ += d.dE[t];
