@@ -315,6 +315,8 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
             diff = __fsub_rn(__fadd_rn((float)d.f2[t], (float)A), (float)wE);
         else
             diff = __dsub_rn(__dadd_rn((double)d.f2[t], (double)A), (double)wE);
+        // the two-test form: the one-band test of the production scan
+        // (acc = __logf(u) - diff < 0) measured 11 % slower here
         const WT l = (WT)d.lf[t];
         const bool acc = store && ((diff >= (WT)0) || (l < diff));
         near |= (diff < (WT)0) && (fabs(l - diff) <= eps);
