@@ -247,6 +247,15 @@ def ours_arm(args, ws, rank, local):
     stream = torch.cuda.Stream()
     eng = m.Engine(L, nchains=chains, device=local, stream=stream.cuda_stream, dev_offset=rank, kernel=args.kernel)
     eng.init_chains(m.INIT_WEIGHT, 0)
+    # the initialisation once more under CUDA events (lattices from the
+    # reference's Philox scheme, then E_J and E_Delta): outside the timed
+    # steps, reported beside them
+    i0, i1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    i0.record(stream)
+    eng.init_chains(m.INIT_WEIGHT, 0)
+    i1.record(stream)
+    i1.synchronize()
+    init_ms = i0.elapsed_time(i1)
     eng.set_weights(np.zeros(N + 1))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
@@ -352,7 +361,7 @@ def ours_arm(args, ws, rank, local):
                              "frac": PHILOX_BLOCKS_PER_ATTEMPT * att_rate / philox_peak,
                              "peak_source": "measured (muca_philox_peak on this GPU)"},
             "roofline_issue": issue_roofline(prof, sweep_avg, clk, eng.info.sms),
-            "sweep_ms": 1e3 * sweep_avg, "gpu_launches": 4 * args.steps,  # per step: the sweep and the three passes of the update
+            "sweep_ms": 1e3 * sweep_avg, "init_ms": init_ms, "gpu_launches": 4 * args.steps,  # per step: the sweep and the three passes of the update
             "clocks": clk, "wall_s_timed_region": t_wall,
         }
     eng.close()

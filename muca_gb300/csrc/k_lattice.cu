@@ -35,12 +35,21 @@ __global__ void k_init(uint32_t *lat, uint32_t L, uint32_t WPR, uint32_t cpb, ui
 {
     const uint32_t words = L * WPR;
     const size_t total = (size_t)((nchains + cpb - 1) / cpb) * cpb * words;
+    const bool narrow = total <= 0xFFFFFFFFull;  // 32-bit index arithmetic (uniform)
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
         // t enumerates [block][word][lane] exactly like the packed layout
-        const uint32_t lane = (uint32_t)(t % cpb);
-        const size_t bw = t / cpb;
-        const uint32_t w = (uint32_t)(bw % words);
-        const uint32_t blk = (uint32_t)(bw / words);
+        uint32_t lane, w, blk;
+        if (narrow) {
+            const uint32_t t32 = (uint32_t)t, bw = t32 / cpb;
+            lane = t32 - bw * cpb;
+            blk = bw / words;
+            w = bw - blk * words;
+        } else {
+            const size_t bw = t / cpb;
+            lane = (uint32_t)(t - bw * cpb);
+            blk = (uint32_t)(bw / words);
+            w = (uint32_t)(bw - (size_t)blk * words);
+        }
         const uint32_t chain = blk * cpb + lane;
         uint32_t word = kZeroWord;
         if (chain < nchains) {
@@ -57,8 +66,7 @@ __global__ void k_init(uint32_t *lat, uint32_t L, uint32_t WPR, uint32_t cpb, ui
                 } else {
                     const uint32_t site = row * L + col, g = site >> 2;
                     if (g != g_cur) {
-                        r = ia.rounds == 10 ? init_block<10>(ia, W, dev, chain, jack, g)
-                                            : init_block<7>(ia, W, dev, chain, jack, g);
+                        r = init_block<R>(ia, W, dev, chain, jack, g);
                         g_cur = g;
                     }
                     const uint32_t rw = pick(r, (int)(site & 3u));

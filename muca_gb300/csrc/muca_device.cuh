@@ -75,11 +75,16 @@ __device__ __forceinline__ float small_int_to_float(int k)
 }
 
 // Initial spin (u < 1/3.0) + (u < 2/3.0) - 1 with the float u compared in
-// double (muca_delta_multigpu.cu:350).
+// double (muca_delta_multigpu.cu:350).  u = k 2^-24 with k = 1 | (r >> 8) is
+// exact in double, and 2^24 times the doubles nearest 1/3 and 2/3 lie
+// strictly inside (5592405, 5592406) and (11184810, 11184811), so the two
+// comparisons are k <= 5592405 and k <= 11184810: integer compares in place
+// of FP64, which issues slowly on this GPU.
+constexpr uint32_t kInitThird = 5592405u, kInitTwoThirds = 11184810u;
 __device__ __forceinline__ int init_spin(uint32_t r)
 {
-    const double u = (double)u01f(r);
-    return (u < 1.0 / 3.0) + (u < 2.0 / 3.0) - 1;
+    const uint32_t k = 1u | (r >> 8);
+    return (int)(k <= kInitThird) + (int)(k <= kInitTwoThirds) - 1;
 }
 
 // Graded initial spin of worker W of `cpd` (an extension): nonzero with

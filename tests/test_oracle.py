@@ -55,6 +55,22 @@ def test_u01_exhaustive_direction_and_init(orc):
         assert (L.orc_u01fixedpt_f32(r) < 0.5) == (r < (1 << 31))
 
 
+def test_init_spin_integer_thresholds():
+    """The device forms the reference's initial spin (u < 1/3.0) +
+    (u < 2/3.0) - 1 (u = u01fixedpt<float>(r) compared in double,
+    muca_delta_multigpu.cu:350) as k <= kInitThird and k <= kInitTwoThirds on
+    k = 1 | (r >> 8); the same for every one of the 2^24 values of k."""
+    import re
+    src = open(os.path.join(os.path.dirname(GOLD), "..", "muca_gb300", "csrc", "muca_device.cuh")).read()
+    m = re.search(r"kInitThird = (\d+)u, kInitTwoThirds = (\d+)u", src)
+    assert m, "thresholds not found in muca_device.cuh"
+    t1, t2 = int(m.group(1)), int(m.group(2))
+    k = np.arange(1 << 24, dtype=np.uint32) | np.uint32(1)
+    u = (k.astype(np.float32) * np.float32(2.0 ** -24)).astype(np.float64)
+    assert np.array_equal(u < 1.0 / 3.0, k <= t1)
+    assert np.array_equal(u < 2.0 / 3.0, k <= t2)
+
+
 def test_acceptance_logf_table_lookup(orc):
     """The table path of the acceptance logarithm: entry r >> 9 holds the value
     for u01fixedpt<float>(r) = (2k+1) 2^-24, so a table of libm's values
