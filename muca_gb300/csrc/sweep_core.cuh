@@ -88,17 +88,18 @@ template <int MODE, int SLOTS, bool HS = true>
 __device__ __forceinline__ void record_window(uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
                                               const int (&Es)[SLOTS], const int (&Ms)[SLOTS], bool checked)
 {
+    // run lengths are at most SLOTS: 32-bit counts, widened at the atomics
     if (MODE == kModeWeight && !HS) {
         int cur = Es[0];
-        unsigned long long cnt = 1;
+        uint32_t cnt = 1;
 #pragma unroll
         for (int t = 1; t < SLOTS; ++t) {
             const bool same = Es[t] == cur;
-            if (!same) atomicAdd(&histG[cur], cnt);
-            cnt = same ? cnt + 1ull : 1ull;
+            if (!same) atomicAdd(&histG[cur], (unsigned long long)cnt);
+            cnt = same ? cnt + 1u : 1u;
             cur = Es[t];
         }
-        atomicAdd(&histG[cur], cnt);
+        atomicAdd(&histG[cur], (unsigned long long)cnt);
     } else if (MODE == kModeWeight) {
         if (checked) {
 #pragma unroll
@@ -114,16 +115,16 @@ __device__ __forceinline__ void record_window(uint32_t *__restrict__ histS, unsi
         for (int t = 0; t < SLOTS; ++t) atomicAdd(&histS[Es[t]], 1u);
     } else {
         uint32_t cur = (uint32_t)(Ms[0] + Es[0] * Es[0] + 2 * Es[0]) >> 1;
-        unsigned long long cnt = 1;
+        uint32_t cnt = 1;
 #pragma unroll
         for (int t = 1; t < SLOTS; ++t) {
             const uint32_t b = (uint32_t)(Ms[t] + Es[t] * Es[t] + 2 * Es[t]) >> 1;
             const bool same = b == cur;
-            if (!same) atomicAdd(&histG[cur], cnt);
-            cnt = same ? cnt + 1ull : 1ull;
+            if (!same) atomicAdd(&histG[cur], (unsigned long long)cnt);
+            cnt = same ? cnt + 1u : 1u;
             cur = b;
         }
-        atomicAdd(&histG[cur], cnt);
+        atomicAdd(&histG[cur], (unsigned long long)cnt);
     }
 }
 
