@@ -181,6 +181,14 @@ const char *muca_last_error(const muca_ctx *ctx);
 muca_status muca_get_info(const muca_ctx *ctx, muca_info *out);
 /* reference NUM_WORKERS formula of the device (muca_delta_multigpu.cu:100-106) */
 muca_status muca_default_chains(int32_t device, uint32_t *out);
+/* Widens the bound of the fast acceptance test (muca_info.log_bracket) to
+ * `bracket`, which must lie between the measured bound and 1e30.  (No
+ * reference counterpart: the reference always evaluates logf.)  Windows
+ * whose decision falls inside the bound are replayed with the exact logf
+ * (and, in production, the FP64 difference); 1e30 sends every window there,
+ * which checks the exact path on its own.  A bound below the measured one is
+ * refused: the fast test could then decide attempts it gets wrong. */
+muca_status muca_set_log_bracket(muca_ctx *ctx, double bracket);
 
 /* Chains.  Replaces the host lattice init (muca_delta_multigpu.cu:340-354,
  * produce2_multigpu.cu:126-140) and computeEnergies/computeDeltaE/computeM

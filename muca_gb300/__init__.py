@@ -30,6 +30,7 @@ STATUS = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "TIMEOUT", 4: "NOT_CONVERGED", 5:
 # Every symbol include/muca.h declares (the C-ABI surface).
 EXPORTS = [
     "muca_create", "muca_destroy", "muca_last_error", "muca_get_info", "muca_default_chains",
+    "muca_set_log_bracket",
     "muca_init_chains", "muca_set_lattice", "muca_get_lattice", "muca_get_chain_state",
     "muca_set_weights", "muca_get_weights", "muca_sweep", "muca_sweep_accumulate",
     "muca_clear_histogram", "muca_get_histogram", "muca_set_histogram", "muca_histogram_stats", "muca_update_weights",
@@ -161,6 +162,7 @@ def lib():
     L.muca_last_error.restype = C.c_char_p
     L.muca_get_info.argtypes = [vp, C.POINTER(Info)]
     L.muca_default_chains.argtypes = [C.c_int32, C.POINTER(C.c_uint32)]
+    L.muca_set_log_bracket.argtypes = [vp, C.c_double]
     L.muca_init_chains.argtypes = [vp, C.c_uint32, C.c_uint32]
     L.muca_set_lattice.argtypes = [vp, i8, C.c_size_t]
     L.muca_get_lattice.argtypes = [vp, i8, C.c_size_t]
@@ -315,6 +317,11 @@ class Engine:
     def sweep(self, iter_, seed_base, seed_dev_mul, therm, nup, accumulate=False):
         f = self._lib.muca_sweep_accumulate if accumulate else self._lib.muca_sweep
         self._ck(f(self._h, iter_, seed_base, seed_dev_mul, therm, nup))
+
+    def set_log_bracket(self, bracket):
+        """Widen the fast acceptance test's bound (1e30: every window takes
+        the exact replay)."""
+        self._ck(self._lib.muca_set_log_bracket(self._h, float(bracket)))
 
     def clear_histogram(self):
         self._ck(self._lib.muca_clear_histogram(self._h))

@@ -46,7 +46,7 @@ struct muca_ctx {
     unsigned long long *d_bad = nullptr, *h_bad = nullptr;
     unsigned int *d_err = nullptr, *h_err = nullptr;
     uint64_t device_bytes = 0;
-    double log_eps = 0;
+    double log_eps = 0, log_eps_measured = 0;
     uint32_t algo = 0;
     float *d_logf_tab = nullptr;  // random-site algorithm with host_logf: the host libm's logf
     std::string err;
@@ -340,6 +340,7 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
         // a finite bound enables the fast test (twice the worst case);
         // anything else keeps every decision on the exact logf
         c->log_eps = (m >= 0.0f && m < 1e-2f) ? 2.0 * (double)m + 1e-30 : 1e30;
+        c->log_eps_measured = c->log_eps;
     }
     if (c->algo == MUCA_ALGO_RANDOM_SITE) {
         if (random_sweep_smem(c->L, c->plan.cpb, false) > c->smem_optin) {
@@ -389,6 +390,16 @@ muca_status muca_get_info(const muca_ctx *c, muca_info *o)
     o->log_bracket = c->log_eps;
     o->kernel = (uint32_t)c->plan.kernel + 1;
     o->threads_per_block = c->plan.threads;
+    return MUCA_OK;
+}
+
+muca_status muca_set_log_bracket(muca_ctx *c, double bracket)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    if (!(bracket >= c->log_eps_measured && bracket <= 1e30))
+        return fail(c, MUCA_ERR_BAD_ARG, "log bracket %g outside [%g, 1e30] (the measured bound and up)", bracket,
+                    c->log_eps_measured);
+    c->log_eps = bracket;
     return MUCA_OK;
 }
 

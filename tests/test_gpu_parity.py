@@ -233,6 +233,48 @@ def test_produce_sweep_vs_oracle(muca, orc, L, cpd, therm, nup, kernel):
     np.testing.assert_array_equal(h, oh)
 
 
+@pytest.mark.parametrize("L,cpd,therm,nup", [(16, 128, 256, 700), (24, 64, 0, 1000), (72, 40, 100, 5184 + 9)])
+@pytest.mark.parametrize("kernel", [2, 3])
+@pytest.mark.parametrize("mode", ["weight", "produce"])
+def test_exact_replay_alone_vs_oracle(muca, orc, L, cpd, therm, nup, kernel, mode):
+    """With the fast test's bound at 1e30 every window of the windowed and
+    warp-specialised kernels takes the exact replay (CUDA's logf; in
+    production also the FP64 difference from the global weights): the
+    oracle's lattices, energies and histograms all the same.  A bound below
+    the measured one is refused."""
+    rng = np.random.default_rng(L * 11 + nup + kernel)
+    N = L * L
+    lnw = _weights(N, rng)
+    produce = mode == "produce"
+    with muca.Engine(L, nchains=cpd, kernel=kernel, mode=muca.MODE_PRODUCE if produce else muca.MODE_WEIGHT) as e:
+        measured = e.info.log_bracket
+        assert 0.0 < measured < 1e-2
+        with pytest.raises(muca.MucaError):
+            e.set_log_bracket(measured * 0.5)
+        with pytest.raises(muca.MucaError):
+            e.set_log_bracket(float("nan"))
+        e.set_log_bracket(1e30)
+        e.set_weights(lnw)
+        e.init_chains(muca.INIT_PRODUCE if produce else muca.INIT_WEIGHT, 0)
+        lat0 = e.get_lattice()
+        ej0, ed0, mg0 = e.chain_state()
+        e.sweep(3, SEED, 2000 if produce else 1000, therm, nup)
+        lat1 = e.get_lattice()
+        ej1, ed1, mg1 = e.chain_state()
+        h = e.histogram()
+    if produce:
+        oej, oed, omg = _ej_ed_copy(ej0), _ej_ed_copy(ed0), _ej_ed_copy(mg0)
+        olat, oh = orc.produce_sweep(L, lat0.copy(), oej, oed, omg, lnw, 3, SEED, therm, nup, nthreads=8)
+        np.testing.assert_array_equal(mg1, omg)
+    else:
+        olat, oej, oed, oh = _oracle_weight_sweep(orc, L, lat0, _ej_ed_copy(ej0), _ej_ed_copy(ed0),
+                                                  lnw.astype(np.float32), 3, therm, nup, 1, cpd)
+    np.testing.assert_array_equal(lat1, olat)
+    np.testing.assert_array_equal(ed1, oed)
+    np.testing.assert_array_equal(ej1, oej)
+    np.testing.assert_array_equal(h, oh)
+
+
 @pytest.mark.parametrize("L,therm,nup,kernel", _with_kernels([(8, 64, 300), (16, 256, 200), (4, 0, 150),
                                                                 (6, 36, 100)]))
 def test_produce_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup, kernel):
