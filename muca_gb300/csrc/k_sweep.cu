@@ -202,8 +202,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
     ChainSetup<MODE, R> cs;
     cs.init(a, cpb, lane, blockIdx.x);
     const uint32_t L = a.L, WPR = a.WPR;
-    // depth 1 or 2 (a power of two): never more than WPR
-    const uint32_t dsh = WPR >= kRingDepth ? 1u : 0u;
+    // depth D: the largest power of two <= min(kRingDepth, WPR)
+    uint32_t dsh = 0;
+    while ((2u << dsh) <= kRingDepth && (2u << dsh) <= WPR) ++dsh;
     const uint32_t D = 1u << dsh;
     const long long deadline = clock64() + kWaitCycles;
     uint32_t w = 0;  // window counter (ring position)
