@@ -212,10 +212,11 @@ __device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32
 }
 
 // The accept/reject scan of a decoded window, its lattice write and its
-// histogram entries.  `store` is false for padding lanes: they read another
+// histogram entries.  ONEBAND (weight mode): decide each attempt with the
+// one-band test of the production scan instead of the two tests.  `store` is false for padding lanes: they read another
 // lane's spins, never accept (so their E stays at 2 and every weight index
 // E + dDel_t + dDel_t+1 stays in [0, 4]) and never write.
-template <int MODE, int SLOTS, bool HS = true>
+template <int MODE, int SLOTS, bool HS = true, bool ONEBAND = false>
 __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, bool store, bool checked,
                                             const typename WeightType<MODE>::T *__restrict__ wS,
                                             uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
@@ -316,11 +317,20 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
             diff = __fsub_rn(__fadd_rn((float)d.f2[t], (float)A), (float)wE);
         else
             diff = __dsub_rn(__dadd_rn((double)d.f2[t], (double)A), (double)wE);
-        // the two-test form: the one-band test of the production scan
-        // (acc = __logf(u) - diff < 0) measured 11 % slower here
         const WT l = (WT)d.lf[t];
-        const bool acc = store && ((diff >= (WT)0) || (l < diff));
-        near |= (diff < (WT)0) && (fabs(l - diff) <= eps);
+        bool acc;
+        if (ONEBAND) {
+            // logf(u) < 0 for every u <= 1 - 2^-24, so  diff >= 0 || logf(u) < diff
+            // is  logf(u) < diff;  g = __logf(u) - diff has its sign unless |g| <= eps
+            const WT g = l - diff;
+            acc = store && (g < (WT)0);
+            near |= fabs(g) <= eps;
+        } else {
+            // two tests: the one-band form measured 11 % slower in the
+            // single-instance kernel (and 1 % faster in the batch kernel)
+            acc = store && ((diff >= (WT)0) || (l < diff));
+            near |= (diff < (WT)0) && (fabs(l - diff) <= eps);
+        }
         if (acc) {
             st.E += d.dDel[t];
             st.EJ += d.dE[t];
@@ -382,7 +392,9 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
 {
     WinDec<MODE> d;
     decode_window<MODE, SLOTS, BT>(lat, cpb, L, WPR, row, q, HALF < 0 ? hrt : (uint32_t)HALF, r1, r3, btab, d);
-    scan_window<MODE, SLOTS, HS>(d, rec, store, checked, wS, histS, histG, st, eps, wG, tol);
+    // the batch kernel (the one user of the beta table) decides weight-mode
+    // attempts with the one-band test
+    scan_window<MODE, SLOTS, HS, BT>(d, rec, store, checked, wS, histS, histG, st, eps, wG, tol);
 }
 
 // The first `len` (< window size) attempts of a window, one at a time as
