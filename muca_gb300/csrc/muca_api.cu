@@ -329,17 +329,9 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
     }
     {
         // the bound of the fast acceptance test, measured once per device
-        static float maxerr_dev[64];
-        static bool have[64];
+        // (cached under a lock: contexts may be created on several threads)
         if (c->device < 0 || c->device >= 64) { fail(c, MUCA_ERR_BAD_ARG, "device %d", c->device); return bail(MUCA_ERR_BAD_ARG); }
-        if (!have[c->device]) {
-            CREATE_TRY(measure_logf_bracket(&maxerr_dev[c->device], c->stream));
-            have[c->device] = true;
-        }
-        const float m = maxerr_dev[c->device];
-        // a finite bound enables the fast test (twice the worst case);
-        // anything else keeps every decision on the exact logf
-        c->log_eps = (m >= 0.0f && m < 1e-2f) ? 2.0 * (double)m + 1e-30 : 1e30;
+        CREATE_TRY(device_log_eps(c->device, c->stream, &c->log_eps));
         c->log_eps_measured = c->log_eps;
     }
     if (c->algo == MUCA_ALGO_RANDOM_SITE) {
