@@ -54,6 +54,7 @@ def test_null_arguments(libmuca):
     assert libmuca.muca_sweep(None, 0, 100, 1000, 16, 16) == 1
     assert libmuca.muca_update_weights(None, 0, None) == 1
     assert libmuca.muca_init_chains(None, 5, 0) == 1
+    assert libmuca.muca_set_log_bracket(None, 1e30) == 1
 
 
 def test_no_gpu_fails_loudly(libmuca):
