@@ -63,7 +63,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ref-gpu", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the flat-run, batch and production lines")
-    p.add_argument("--only", choices=["flat_run", "batch", "production"],
+    p.add_argument("--only", choices=["flat_run", "batch", "production", "random_site"],
                    help="run only this extra line and print it (for profiling a smaller case)")
     p.add_argument("--production-L", type=int, default=128, help="lattice size of --only production")
     p.add_argument("--kernel", type=int, default=0, help="sweep kernel: 0 auto, 1 generic, 2 windowed, 3 specialised")
@@ -368,7 +368,8 @@ def ours_arm(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_ref_gpu:
         out["ref_gpu_kernel"] = ref_gpu_kernel_rate(L, chains)
     if rank == 0 and ws == 1 and not args.no_extra:
-        for key, fn in (("flat_run", flat_run_metric), ("batch", batch_metric), ("production", production_metric)):
+        for key, fn in (("flat_run", flat_run_metric), ("batch", batch_metric), ("production", production_metric),
+                        ("random_site", random_site_metric)):
             try:
                 out[key] = fn(local)
             except Exception as ex:  # an extra line never fails the bench
@@ -430,6 +431,69 @@ def batch_metric(local, iters=32):
                       "hist_in_smem": info.shape.hist_in_smem, "blocks_per_sm": info.shape.blocks_per_sm,
                       "shapes_tried": info.n_tried},
             "graph": "%d iterations (clear, persistent sweep, update) per CUDA graph" % iters}
+
+
+def random_site_metric(local, L=72, nc=16384):
+    """The CPU weight program's random-site algorithm (muca_mag.cpp:312-393:
+    random site, three Philox streams, FP64 weights) on the device
+    (MUCA_ALGO_RANDOM_SITE), at the headline's L and chain count: one sweep
+    of therm = N and nup = N attempts per chain, CUDA events around the
+    launch (best of 3 after a warm-up).  host_logf 0 decides with CUDA's
+    logf (the reference's mcs2), 1 with the host libm's (bit-exact with the
+    CPU program).  Beside it, the oracle's restatement of muca_mag's mcs on
+    every chain with all host threads: the reference CPU algorithm."""
+    import numpy as np
+    import torch
+    import muca_gb300 as m
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import orc
+    N = L * L
+    att = nc * 2 * N
+    out = {"metric": "random-site sweep attempts/ns at L=%d (the CPU weight program's algorithm)" % L,
+           "unit": "attempts/ns", "chains": nc, "attempts_per_chain": 2 * N,
+           "timing": "CUDA events around one sweep launch, best of 3 after a warm-up; zero weights"}
+    stream = torch.cuda.Stream()
+    for hl, key in ((0, "cuda_logf"), (1, "host_logf")):
+        with m.Engine(L, nchains=nc, device=local, algorithm=m.ALGO_RANDOM_SITE, host_logf=hl,
+                      stream=stream.cuda_stream) as e:
+            e.set_weights(np.zeros(N + 1))
+            e.init_chains(m.INIT_MUCA_MAG, 0)
+            e.sweep(0, 0, 0, N, N)
+            best = None
+            for k in range(3):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                e.sweep(k + 1, 0, 0, N, N)
+                b.record(stream)
+                b.synchronize()
+                t = a.elapsed_time(b)
+                best = t if best is None else min(best, t)
+        out[key] = att / (best * 1e6)
+        out[key + "_ms"] = best
+    # the oracle's muca_mag mcs over every chain, all host threads (ctypes
+    # releases the interpreter lock during each call)
+    Lb = orc.lib()
+    lat = orc.init_lattice(L, nc, orc.scheme_muca_mag(0))
+    ej, ed, _ = orc.energies(L, lat)
+    lnw = np.zeros(N + 1)
+    nthreads = os.cpu_count() or 1
+
+    def chains(lo, hi):
+        hc = np.zeros(N + 1, np.uint64)
+        e1 = np.zeros(1, np.int32)
+        e2 = np.zeros(1, np.int32)
+        for c in range(lo, hi):
+            e1[0], e2[0] = ej[c], ed[c]
+            Lb.orc_muca_mag_mcs(L, c, lat[c], e1, e2, lnw, hc, 1, 0, N, N)
+
+    bounds = np.linspace(0, nc, nthreads + 1).astype(int)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(nthreads) as ex:
+        list(ex.map(lambda i: chains(bounds[i], bounds[i + 1]), range(nthreads)))
+    dt = time.perf_counter() - t0
+    out["cpu"] = {"value": att / (dt * 1e9), "unit": "attempts/ns", "cores": nthreads, "kind": "port",
+                  "sample": "all %d chains, one sweep (therm N + nup N), %.1f s wall" % (nc, dt)}
+    return out
 
 
 def production_metric(local, L=128, with_ref=True, kernel=0):
@@ -526,7 +590,7 @@ def main():
         torch.cuda.set_device(local)
         from muca_gb300 import build as b
         b.build()
-        fn = {"flat_run": flat_run_metric, "batch": batch_metric,
+        fn = {"flat_run": flat_run_metric, "batch": batch_metric, "random_site": random_site_metric,
               "production": lambda d: production_metric(d, args.production_L, with_ref=False, kernel=args.kernel)}[args.only]
         print(json.dumps(fn(local)))
         return 0
