@@ -26,6 +26,12 @@ weight update on the device.  Spins start from the reference initialisation
   cpu_baseline  the CPU oracle (the reference algorithm restated in C, one
                 chain per thread task, all host threads) on full steps.
 
+Beside the headline the default line carries `flat_run` (iterations and time
+to a flat histogram), `batch` (256 uneven instances), `production` (L=128
+with its reweighting) and `random_site` (the CPU weight program's algorithm
+on the device, with the oracle's restatement of it on the host threads);
+`--only NAME` prints one of them alone.
+
 `--impl reference` times the reference's CPU algorithm (the oracle port: the
 reference CPU sources cannot be built on the GPU host) on the same workload.
 With N > 1 processes (torchrun), every rank runs its own shard as reference
