@@ -190,6 +190,23 @@ muca_status muca_default_chains(int32_t device, uint32_t *out);
  * refused: the fast test could then decide attempts it gets wrong. */
 muca_status muca_set_log_bracket(muca_ctx *ctx, double bracket);
 
+/* Failure detection (no reference counterpart: the reference's only check is
+ * cudaGetLastError, muca_delta_multigpu.cu:417-421, and its iteration loop has
+ * no cap, :374).  Every device-side wait of the warp-specialised sweep gives
+ * up after `cycles` SM clock cycles without progress (0 = the default 2^34,
+ * about 8 s at 2 GHz; at most 2^40); the launch then ends normally, sets the
+ * context's error word, and the next synchronising call returns
+ * MUCA_ERR_TIMEOUT (and clears the word, so the context stays usable; the
+ * chains' state after such a launch is not valid).  The bound is per wait, so
+ * a long launch that keeps making progress never times out. */
+muca_status muca_set_wait_limit(muca_ctx *ctx, uint64_t cycles);
+/* Test hooks, for tests of the timeout path only (0 in normal use).
+ * MUCA_HOOK_SILENT_PRODUCER: the producer warps of the warp-specialised sweep
+ * never signal a filled ring slot, so the consumers' bounded waits run out.
+ * Nothing faults and every wait stays bounded. */
+#define MUCA_HOOK_SILENT_PRODUCER 1u
+muca_status muca_set_test_hooks(muca_ctx *ctx, uint32_t hooks);
+
 /* Chains.  Replaces the host lattice init (muca_delta_multigpu.cu:340-354,
  * produce2_multigpu.cu:126-140) and computeEnergies/computeDeltaE/computeM
  * (muca_delta_multigpu.cu:69-83, produce2_multigpu.cu:66-89), on the device. */
@@ -272,13 +289,19 @@ muca_status muca_compute_observables(muca_ctx *ctx, double beta, double delta, m
  * nothing: for callers that must not see a device allocation (a scheduler
  * owning HBM through its own pool and budget; a process that only reweights
  * histograms it holds).  Its scratch is a fixed device array of 304 x 4
- * doubles inside the library, whose address is looked up on the first call
- * per device; make that first call before any stream capture, since it may
- * load the module.  Nothing needs to start at zero.  Two calls in flight at
+ * doubles inside the library (the partials of a fixed 304-block grid; the
+ * size does not depend on L), whose address is looked up on the first call
+ * per device and cached; make that first call before any stream capture,
+ * since it may load the module.  The cached address belongs to the device's
+ * current context: after cudaDeviceReset (or anything else that destroys the
+ * primary context) it is stale, so do not call this entry point again in
+ * that process.  Nothing needs to start at zero.  Two calls in flight at
  * once on the same device share that array and race.  L outside 2..128 is
- * rejected with MUCA_ERR_BAD_ARG.  The work is enqueued on `stream`
- * (cudaStream_t, NULL = the legacy default stream); d_sums is valid once the
- * stream reaches it.  Errors: muca_last_error(NULL). */
+ * rejected with MUCA_ERR_BAD_ARG: that is the library-wide range of L
+ * (muca_create checks the same), not a limit of the scratch.  The caller's current
+ * device is the same after the call as before.  The work is enqueued on
+ * `stream` (cudaStream_t, NULL = the legacy default stream); d_sums is valid
+ * once the stream reaches it.  Errors: muca_last_error(NULL). */
 muca_status muca_observables_noalloc(int32_t device, const uint64_t *d_hist2d, const double *d_lnw, uint32_t L,
                                     double beta, double delta, double *d_sums, void *stream);
 /* Leave-one-out jackknife (muca_delta_multigpu.cu:620-635) on the device. */

@@ -25,12 +25,13 @@ INIT_WEIGHT, INIT_PRODUCE, INIT_CHAIN_COUNTER, INIT_ORDERED, INIT_MUCA_MAG, INIT
 ALGO_SWEEP, ALGO_RANDOM_SITE = 0, 1
 UPDATE_TRIVIAL, UPDATE_TRIVIAL_CPU, UPDATE_RECURSION = 0, 1, 2
 KERNEL_AUTO, KERNEL_GENERIC, KERNEL_WINDOWED, KERNEL_SPECIALIZED = 0, 1, 2, 3
+HOOK_SILENT_PRODUCER = 1
 STATUS = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "TIMEOUT", 4: "NOT_CONVERGED", 5: "IO", 6: "STATE"}
 
 # Every symbol include/muca.h declares (the C-ABI surface).
 EXPORTS = [
     "muca_create", "muca_destroy", "muca_last_error", "muca_get_info", "muca_default_chains",
-    "muca_set_log_bracket",
+    "muca_set_log_bracket", "muca_set_wait_limit", "muca_set_test_hooks",
     "muca_init_chains", "muca_set_lattice", "muca_get_lattice", "muca_get_chain_state",
     "muca_set_weights", "muca_get_weights", "muca_sweep", "muca_sweep_accumulate",
     "muca_clear_histogram", "muca_get_histogram", "muca_set_histogram", "muca_histogram_stats", "muca_update_weights",
@@ -163,6 +164,8 @@ def lib():
     L.muca_get_info.argtypes = [vp, C.POINTER(Info)]
     L.muca_default_chains.argtypes = [C.c_int32, C.POINTER(C.c_uint32)]
     L.muca_set_log_bracket.argtypes = [vp, C.c_double]
+    L.muca_set_wait_limit.argtypes = [vp, C.c_uint64]
+    L.muca_set_test_hooks.argtypes = [vp, C.c_uint32]
     L.muca_init_chains.argtypes = [vp, C.c_uint32, C.c_uint32]
     L.muca_set_lattice.argtypes = [vp, i8, C.c_size_t]
     L.muca_get_lattice.argtypes = [vp, i8, C.c_size_t]
@@ -322,6 +325,15 @@ class Engine:
         """Widen the fast acceptance test's bound (1e30: every window takes
         the exact replay)."""
         self._ck(self._lib.muca_set_log_bracket(self._h, float(bracket)))
+
+    def set_wait_limit(self, cycles):
+        """Bound of every device-side wait of the warp-specialised sweep, in
+        SM clock cycles without progress (0 = the default, about 8 s)."""
+        self._ck(self._lib.muca_set_wait_limit(self._h, int(cycles)))
+
+    def set_test_hooks(self, hooks):
+        """Test hooks of the timeout path (HOOK_SILENT_PRODUCER); 0 = none."""
+        self._ck(self._lib.muca_set_test_hooks(self._h, int(hooks)))
 
     def clear_histogram(self):
         self._ck(self._lib.muca_clear_histogram(self._h))

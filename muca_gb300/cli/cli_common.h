@@ -59,6 +59,91 @@ inline void die(const char *what, muca_ctx *c)
     std::exit(1);
 }
 
+// Weight files.  The reference reads them unchecked: a missing file only
+// prints "!error!" and the run goes on with zero weights
+// (produce2_multigpu.cu:210-213), a short or non-numeric file leaves zeros
+// where the read stopped, and the while(!eof) loop writes one entry past the
+// array on a trailing newline (:216-220; the continuing file, one value per
+// line, :223-235).  Here a file must hold exactly N+1 finite values (for
+// the pair format, "i lnW" with i = 0..N in order); anything else is
+// reported with the first offending token and the program exits with
+// status 3 before it touches the GPU.
+inline bool read_tokens(const std::string &path, std::vector<std::string> &tok, std::string &why)
+{
+    FILE *f = std::fopen(path.c_str(), "r");
+    if (!f) {
+        why = path + ": cannot open";
+        return false;
+    }
+    char buf[256];
+    while (std::fscanf(f, "%255s", buf) == 1) tok.emplace_back(buf);
+    std::fclose(f);
+    return true;
+}
+
+inline bool parse_real(const std::string &t, double &v)
+{
+    char *end = nullptr;
+    v = std::strtod(t.c_str(), &end);
+    return end && *end == '\0' && end != t.c_str() && std::isfinite(v);
+}
+
+// "i lnW" pairs (produce2_multigpu.cu:214-220)
+inline bool read_weight_pairs(const std::string &path, unsigned N, std::vector<double> &w, std::string &why)
+{
+    std::vector<std::string> tok;
+    if (!read_tokens(path, tok, why)) return false;
+    w.assign((size_t)N + 1, 0.0);
+    for (size_t k = 0; k < tok.size(); k += 2) {
+        const size_t i = k / 2;
+        char *end = nullptr;
+        const long idx = std::strtol(tok[k].c_str(), &end, 10);
+        if (!end || *end != '\0' || idx != (long)i) {
+            why = path + ": entry " + std::to_string(i) + ": index '" + tok[k] + "' (expected " +
+                  std::to_string(i) + ")";
+            return false;
+        }
+        if (i > N) {
+            why = path + ": more than N+1 = " + std::to_string(N + 1) + " entries";
+            return false;
+        }
+        if (k + 1 >= tok.size() || !parse_real(tok[k + 1], w[i])) {
+            why = path + ": entry " + std::to_string(i) + ": value '" + (k + 1 < tok.size() ? tok[k + 1] : "") +
+                  "' is not a finite number";
+            return false;
+        }
+    }
+    if (tok.size() != 2 * ((size_t)N + 1)) {
+        why = path + ": " + std::to_string(tok.size() / 2) + " entries, expected N+1 = " + std::to_string(N + 1);
+        return false;
+    }
+    return true;
+}
+
+// one value per line (the continuing file, muca_delta_multigpu.cu:223-235)
+inline bool read_weight_column(const std::string &path, unsigned N, std::vector<double> &w, std::string &why)
+{
+    std::vector<std::string> tok;
+    if (!read_tokens(path, tok, why)) return false;
+    if (tok.size() != (size_t)N + 1) {
+        why = path + ": " + std::to_string(tok.size()) + " values, expected N+1 = " + std::to_string(N + 1);
+        return false;
+    }
+    w.assign((size_t)N + 1, 0.0);
+    for (size_t i = 0; i <= N; ++i)
+        if (!parse_real(tok[i], w[i])) {
+            why = path + ": value " + std::to_string(i) + " '" + tok[i] + "' is not a finite number";
+            return false;
+        }
+    return true;
+}
+
+inline void die_io(const std::string &why)
+{
+    std::fprintf(stderr, "error: weight file: %s\n", why.c_str());
+    std::exit(3);
+}
+
 // ./fss/L<L> is where the reference programs read and write their files.
 inline void ensure_dir(const std::string &d)
 {

@@ -81,6 +81,13 @@ int main(int argc, char **argv)
         std::fprintf(stderr, "error: invalid arguments\n");
         return 2;
     }
+    const unsigned N = L * L;
+    std::vector<double> log_weight((size_t)N + 1, 0.0);
+    if (extrapolation) {  // :223-235, one value per line; checked before any device work
+        std::string why;
+        if (!cli::read_weight_column("./fss/L" + Ls + "/initweight_L128_T050.txt", N, log_weight, why))
+            cli::die_io(why);
+    }
     const int device = (int)opt.num("device", starting_gpu);
     uint32_t NUM_WORKERS = 0;
     if (opt.has("chains")) {
@@ -102,14 +109,8 @@ int main(int argc, char **argv)
     prm.kernel = (uint32_t)opt.num("kernel", 0);
     muca_ctx *ctx = nullptr;
     if (muca_create(&prm, &ctx) != MUCA_OK) cli::die("create", nullptr);
-    const unsigned N = L * L;
     cli::ensure_dir("./fss/L" + Ls);
 
-    std::vector<double> log_weight(N + 1, 0.0);
-    if (extrapolation) {  // :223-235, one value per line
-        std::ifstream initweightfile(("./fss/L" + Ls + "/initweight_L128_T050.txt").c_str());
-        for (unsigned i = 0; i <= N; i++) initweightfile >> log_weight[i];
-    }
     if (muca_set_weights(ctx, log_weight.data(), N + 1) != MUCA_OK) cli::die("set weights", ctx);
 
     const unsigned therm_coeff = 1;

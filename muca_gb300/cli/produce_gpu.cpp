@@ -63,6 +63,15 @@ int main(int argc, char **argv)
     }
     const bool blocks = opt.has("jack-blocks") && JACKS > 0;
     const bool reuse = opt.has("reuse-histogram");
+    const unsigned N = L * L;
+    // weight file: "i lnW" pairs (:205-226), checked before any device work
+    std::vector<double> log_weight;
+    {
+        std::string why;
+        if (!cli::read_weight_pairs("./fss/L" + Ls + "/weight_mpi_T050c16_M200_JACK0_DKL1e-4.txt", N, log_weight,
+                                    why))
+            cli::die_io(why);
+    }
     const int device = (int)opt.num("device", first_gpu);
     uint32_t NUM_WORKERS = 0;
     if (opt.has("chains")) {
@@ -70,7 +79,6 @@ int main(int argc, char **argv)
     } else if (muca_default_chains(device, &NUM_WORKERS) != MUCA_OK) {
         cli::die("device query", nullptr);
     }
-    const unsigned N = L * L;
 
     // one context per emulated device: each has its own 2D histogram
     std::vector<muca_ctx *> ctx(NofGPU, nullptr);
@@ -89,21 +97,6 @@ int main(int argc, char **argv)
     }
     cli::ensure_dir("./fss/L" + Ls);
 
-    // weight file: "i lnW" pairs read until they stop (:214-220)
-    std::vector<double> log_weight(N + 1, 0.0);
-    {
-        std::ifstream inFile(("./fss/L" + Ls + "/weight_mpi_T050c16_M200_JACK0_DKL1e-4.txt").c_str());
-        if (inFile.fail()) std::cout << "!error!" << std::endl;
-        int idx;
-        double w;
-        unsigned num = 0;
-        while (inFile >> idx >> w) {
-            if (num <= N) log_weight[num] = w;
-            ++num;
-        }
-        if (num && num < N + 1)
-            std::fprintf(stderr, "warning: weight file holds %u of %u values; the rest are 0\n", num, N + 1);
-    }
     for (unsigned g = 0; g < NofGPU; ++g)
         if (muca_set_weights(ctx[g], log_weight.data(), N + 1) != MUCA_OK) cli::die("set weights", ctx[g]);
 

@@ -79,15 +79,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
         : "memory");
     return ok != 0;
 }
-// Bounded wait: gives up (returns false) once clock64() passes `deadline`.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long deadline)
+// Bounded wait: gives up once the phase has not completed for `limit` SM
+// clock cycles (measured from this wait's start, so a long launch that keeps
+// making progress never gives up).  Every lane of the calling warp waits on
+// the same barrier at the same point; the outcome is voted across the warp,
+// so a warp never splits between giving up and going on (the scan's
+// warp-wide votes need all 32 lanes).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit)
 {
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() > deadline) return false;
-    return true;
+    bool done = mbar_try_wait(bar, parity);
+    if (!done) {
+        const long long t0 = clock64();
+        while (!(done = mbar_try_wait(bar, parity)))
+            if (clock64() - t0 > limit) break;
+    }
+    return __all_sync(0xffffffffu, done);
 }
-
-constexpr long long kWaitCycles = 1ll << 34;  // ~8 s at 2 GHz; a normal launch takes milliseconds
 
 // Slot words (index f: shared u32 at slot[32 f], one column per lane).
 enum SlotWord : uint32_t {
@@ -206,7 +213,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
     uint32_t dsh = 0;
     while ((2u << dsh) <= kRingDepth && (2u << dsh) <= WPR) ++dsh;
     const uint32_t D = 1u << dsh;
-    const long long deadline = clock64() + kWaitCycles;
+    const long long limit = a.wait_cycles > 0 ? a.wait_cycles : kWaitCyclesDefault;
+    const bool silent = (a.hooks & kHookSilentProducer) != 0;
     uint32_t w = 0;  // window counter (ring position)
     bool ok = true;
 
@@ -225,11 +233,11 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
                 // a new half or phase: the windows still in the ring must be written back
                 for (uint32_t j = 1; j < D && j <= w; ++j) {
                     const uint32_t v = w - j;
-                    if (!mbar_wait(empty + (v & (D - 1u)), (v >> dsh) & 1u, deadline)) { ok = false; return false; }
+                    if (!mbar_wait(empty + (v & (D - 1u)), (v >> dsh) & 1u, limit)) { ok = false; return false; }
                 }
             }
             const uint32_t s = w & (D - 1u), round = w >> dsh;
-            if (!mbar_wait(empty + s, (round & 1u) ^ 1u, deadline)) { ok = false; return false; }
+            if (!mbar_wait(empty + s, (round & 1u) ^ 1u, limit)) { ok = false; return false; }
             uint32_t *slot = myring + (size_t)s * kSlotWords * 32;
             if (len < cnt) {
 #pragma unroll
@@ -243,7 +251,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
                 decode_window<MODE, 4>(lat, cpb, L, WPR, row, q, half, r1, r3, nullptr, d);
                 put_window<MODE, 4>(d, slot);
             }
-            mbar_arrive(full + s);
+            if (!silent) mbar_arrive(full + s);
             ++w;
             return true;
         });
@@ -258,7 +266,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
         for_each_window(L, WPR, a.therm, nup, [&](uint32_t row, uint32_t q, uint32_t half, uint32_t cnt,
                                                   uint32_t len, bool rec_phase) {
             const uint32_t s = w & (D - 1u), round = w >> dsh;
-            if (!mbar_wait(full + s, round & 1u, deadline)) { ok = false; return false; }
+            if (!mbar_wait(full + s, round & 1u, limit)) { ok = false; return false; }
             const uint32_t *slot = myring + (size_t)s * kSlotWords * 32;
             const bool rec = rec_phase && cs.active;
             uint32_t *pc = lat + (size_t)(row * WPR + q) * cpb;

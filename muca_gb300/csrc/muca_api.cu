@@ -49,6 +49,8 @@ struct muca_ctx {
     double log_eps = 0, log_eps_measured = 0;
     uint32_t algo = 0;
     float *d_logf_tab = nullptr;  // random-site algorithm with host_logf: the host libm's logf
+    long long wait_cycles = 0;    // bound of the sweep's device-side waits (0 = default)
+    uint32_t hooks = 0;           // test hooks of the sweep (kHook*)
     std::string err;
 };
 
@@ -171,6 +173,8 @@ SweepArgs sweep_args(muca_ctx *c, uint32_t iter, uint32_t seed_base, uint32_t se
     a.log_eps = c->log_eps;
     a.err = c->d_err;
     a.dyn = nullptr;
+    a.wait_cycles = c->wait_cycles;
+    a.hooks = c->hooks;
     return a;
 }
 
@@ -392,6 +396,24 @@ muca_status muca_set_log_bracket(muca_ctx *c, double bracket)
         return fail(c, MUCA_ERR_BAD_ARG, "log bracket %g outside [%g, 1e30] (the measured bound and up)", bracket,
                     c->log_eps_measured);
     c->log_eps = bracket;
+    return MUCA_OK;
+}
+
+muca_status muca_set_wait_limit(muca_ctx *c, uint64_t cycles)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    if (cycles > (1ull << 40)) return fail(c, MUCA_ERR_BAD_ARG, "wait limit %llu cycles above 2^40",
+                                           (unsigned long long)cycles);
+    c->wait_cycles = (long long)cycles;
+    return MUCA_OK;
+}
+
+muca_status muca_set_test_hooks(muca_ctx *c, uint32_t hooks)
+{
+    if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
+    if (hooks & ~(uint32_t)MUCA_HOOK_SILENT_PRODUCER) return fail(c, MUCA_ERR_BAD_ARG, "unknown hook bits 0x%x", hooks);
+    static_assert(MUCA_HOOK_SILENT_PRODUCER == kHookSilentProducer, "hook bits");
+    c->hooks = hooks;
     return MUCA_OK;
 }
 
@@ -888,9 +910,19 @@ muca_status muca_observables_noalloc(int32_t device, const uint64_t *d_hist2d, c
     if (observables_partials(N) > observables_static_partials())
         return fail(nullptr, MUCA_ERR_BAD_ARG, "L=%u needs %zu doubles of scratch; the static array holds %zu", L,
                     observables_partials(N), observables_static_partials());
-    CUDA_TRY(nullptr, cudaSetDevice(device));
-    CUDA_TRY(nullptr, launch_observables_static(device, reinterpret_cast<const unsigned long long *>(d_hist2d), d_lnw,
-                                                N, beta, delta, d_sums, static_cast<cudaStream_t>(stream)));
+    // the caller's current device is put back on every return path: a
+    // scheduler driving several GPUs from one thread keeps its own choice
+    int prev = -1;
+    CUDA_TRY(nullptr, cudaGetDevice(&prev));
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess)
+        e = launch_observables_static(device, reinterpret_cast<const unsigned long long *>(d_hist2d), d_lnw, N, beta,
+                                      delta, d_sums, static_cast<cudaStream_t>(stream));
+    const cudaError_t er = prev != device ? cudaSetDevice(prev) : cudaSuccess;
+    if (e != cudaSuccess) return fail(nullptr, MUCA_ERR_CUDA, "observables_noalloc: %s", cudaGetErrorString(e));
+    if (er != cudaSuccess)
+        return fail(nullptr, MUCA_ERR_CUDA, "observables_noalloc: restoring device %d: %s", prev,
+                    cudaGetErrorString(er));
     return MUCA_OK;
 }
 

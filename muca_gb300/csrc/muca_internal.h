@@ -33,7 +33,19 @@ struct SweepArgs {
     const uint32_t *dyn;
     // error word: bit 0 is set when a bounded wait inside a kernel gave up
     unsigned int *err;
+    // bound of every device-side wait (warp-specialised kernel), in SM clock
+    // cycles without progress; 0 = kWaitCyclesDefault
+    long long wait_cycles;
+    // test hooks (kHook*); 0 in normal operation
+    uint32_t hooks;
 };
+// ~8 s at 2 GHz without progress: a healthy wait completes in microseconds
+constexpr long long kWaitCyclesDefault = 1ll << 34;
+// kHookSilentProducer: the producer warps of the warp-specialised sweep never
+// signal a filled ring slot, so the consumers' bounded waits run out and the
+// launch ends with the error word set (a test of the timeout path; it faults
+// nothing and every wait stays bounded)
+constexpr uint32_t kHookSilentProducer = 1u;
 
 enum SweepMode { kModeWeight = 0, kModeProduce = 1 };
 

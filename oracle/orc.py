@@ -46,9 +46,21 @@ class WeightOpts(C.Structure):
                 ("algo", C.c_uint)]
 
 
+def reference_dir() -> str:
+    """The reference checkout the recipe reads: $MUCA_REFERENCE, else the
+    recipe's own REF (oracle/Makefile).  It exists only where the reference
+    was checked out; nothing on the GPU host needs it."""
+    env = os.environ.get("MUCA_REFERENCE")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], stdout=subprocess.PIPE, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
 def build(ref: bool = False, refgpu: bool = False) -> None:
     targets = ["oracle"] + (["refgpu"] if refgpu else []) + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE, "-j8"] + targets, check=True)
+    extra = ["REF=" + os.environ["MUCA_REFERENCE"]] if ref and os.environ.get("MUCA_REFERENCE") else []
+    subprocess.run(["make", "-s", "-C", HERE, "-j8"] + targets + extra, check=True)
 
 
 _LIB = None

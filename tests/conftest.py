@@ -53,9 +53,17 @@ def muca():
 @pytest.fixture(scope="session")
 def refgpu(orc):
     """Launcher of the reference kernels (cubins compiled from the reference
-    sources); None when the cubins are not present in this checkout."""
+    sources).  Where the cubins are missing the tests that need them skip,
+    unless MUCA_REQUIRE_REF_KERNELS=1 says they must be there: then they fail."""
     try:
         orc.build(refgpu=True)
-    except Exception:
-        return None
-    return orc.refgpu()
+        launcher = orc.refgpu()
+    except Exception as ex:  # noqa: BLE001
+        launcher, why = None, str(ex)
+    else:
+        why = "reference cubins not present in this checkout"
+    if launcher is None:
+        if os.environ.get("MUCA_REQUIRE_REF_KERNELS") == "1":
+            pytest.fail("reference kernels required (MUCA_REQUIRE_REF_KERNELS=1): " + why)
+        pytest.skip(why)
+    return launcher

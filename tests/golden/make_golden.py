@@ -1,7 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the reference.
 
-Run in a checkout where the reference is available (default /root/reference,
-or $MUCA_REFERENCE) after `make -C oracle ref`:
+Run in a checkout where the reference is available ($MUCA_REFERENCE, else
+the REF of oracle/Makefile) after `make -C oracle ref`:
 
     python tests/golden/make_golden.py
 
@@ -34,7 +34,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from oracle import orc  # noqa: E402
 
-REF = os.environ.get("MUCA_REFERENCE", "/root/reference")
+REF = orc.reference_dir()
+if not REF or not os.path.isdir(REF):
+    sys.exit("make_golden.py: the reference checkout %r does not exist; set MUCA_REFERENCE" % REF)
 
 
 def philox_kat():

@@ -55,6 +55,8 @@ def test_null_arguments(libmuca):
     assert libmuca.muca_update_weights(None, 0, None) == 1
     assert libmuca.muca_init_chains(None, 5, 0) == 1
     assert libmuca.muca_set_log_bracket(None, 1e30) == 1
+    assert libmuca.muca_set_wait_limit(None, 1000) == 1
+    assert libmuca.muca_set_test_hooks(None, 0) == 1
 
 
 def test_no_gpu_fails_loudly(libmuca):

@@ -290,3 +290,72 @@ def test_multigpu_weight_recursion_matches_oracle(exes, orc, tmp_path):
     rows = [ln.split() for ln in (d / ("shortiter_gpu1_T050c%d_M1_therm1N_Jack0_iterupdate1.01_rand.txt" % NW))
             .read_text().splitlines()[1:]]
     _check_log(rows, it, rec)
+
+
+# ---- malformed weight files (host side, before any device work) ------------------------------
+
+def _weight_pairs(L, lnw):
+    return "".join("%d %.10g\n" % (i, v) for i, v in enumerate(lnw))
+
+
+@pytest.mark.parametrize("case", ["missing", "truncated", "non_numeric", "nan", "index", "extra", "empty"])
+def test_produce_gpu_rejects_malformed_weight_file(exes, tmp_path, case):
+    """The reference reads the weight file unchecked (produce2_multigpu.cu:210-220):
+    a missing file prints "!error!" and runs on zero weights, a short or
+    non-numeric one leaves zeros, a trailing newline writes past the array.
+    The drop-in refuses such a file with status 3 and names the problem,
+    before it touches the GPU (so this runs without one)."""
+    L = 4
+    N = L * L
+    d = tmp_path / "fss" / ("L%d" % L)
+    d.mkdir(parents=True)
+    lnw = -0.5 * np.arange(N + 1)
+    body = _weight_pairs(L, lnw)
+    lines = body.splitlines(keepends=True)
+    if case == "truncated":
+        body = "".join(lines[:-3])
+    elif case == "non_numeric":
+        lines[5] = "5 abc\n"
+        body = "".join(lines)
+    elif case == "nan":
+        lines[7] = "7 nan\n"
+        body = "".join(lines)
+    elif case == "index":
+        lines[3] = "4 -1.5\n"
+        body = "".join(lines)
+    elif case == "extra":
+        body = body + "%d 0\n" % (N + 1)
+    elif case == "empty":
+        body = "\n"
+    if case != "missing":
+        (d / "weight_mpi_T050c16_M200_JACK0_DKL1e-4.txt").write_text(body)
+    args = [str(L), "0", "0", "1", "1", "1", "1", "1.9", "0.1", "--chains=64"]
+    r = subprocess.run([exes[1]] + args, capture_output=True, text=True, cwd=tmp_path, timeout=120)
+    assert r.returncode == 3, (r.returncode, r.stderr)
+    assert "weight file" in r.stderr
+    expect = {"missing": "cannot open", "truncated": "entries, expected N+1 = 17", "non_numeric": "'abc'",
+              "nan": "'nan'", "index": "index '4' (expected 3)", "extra": "more than N+1",
+              "empty": "0 entries"}[case]
+    assert expect in r.stderr, r.stderr
+
+
+@pytest.mark.parametrize("case", ["truncated", "non_numeric", "missing"])
+def test_multigpu_weight_rejects_malformed_initial_weight(exes, tmp_path, case):
+    """The continuing path's initial weight (one value per line,
+    muca_delta_multigpu.cu:223-235) must hold N+1 finite values."""
+    L = 4
+    N = L * L
+    d = tmp_path / "fss" / ("L%d" % L)
+    d.mkdir(parents=True)
+    vals = ["%.10g" % (-0.25 * i) for i in range(N + 1)]
+    if case == "truncated":
+        vals = vals[:N]
+    elif case == "non_numeric":
+        vals[2] = "x1"
+    if case != "missing":
+        (d / "initweight_L128_T050.txt").write_text("\n".join(vals) + "\n")
+    r = subprocess.run([exes[0], str(L), "0", "0", "1", "1", "0", "1", "--chains=64", "--max-iter=2"],
+                       capture_output=True, text=True, cwd=tmp_path, timeout=120)
+    assert r.returncode == 3, (r.returncode, r.stderr)
+    expect = {"truncated": "16 values, expected N+1 = 17", "non_numeric": "'x1'", "missing": "cannot open"}[case]
+    assert expect in r.stderr, r.stderr

@@ -149,8 +149,6 @@ def test_weight_sweep_vs_oracle(muca, orc, L, cpd, ndev, therm, nup, kernel):
                                                                 (72, 5184, 41), (4, 16, 200), (6, 36, 99),
                                                                 (10, 100, 57)]))
 def test_weight_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup, kernel):
-    if refgpu is None:
-        pytest.skip("reference cubins not present in this checkout")
     rng = np.random.default_rng(L + 7)
     N = L * L
     lnw = _weights(N, rng)
@@ -174,8 +172,6 @@ def test_weight_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup, kern
 
 def test_reference_kernel_init_energies(muca, orc, refgpu):
     """computeEnergies/computeDeltaE of the reference against ours."""
-    if refgpu is None:
-        pytest.skip("reference cubins not present in this checkout")
     L = 16
     with muca.Engine(L, nchains=256) as e:
         e.init_chains(muca.INIT_WEIGHT, 0)
@@ -278,8 +274,6 @@ def test_exact_replay_alone_vs_oracle(muca, orc, L, cpd, therm, nup, kernel, mod
 @pytest.mark.parametrize("L,therm,nup,kernel", _with_kernels([(8, 64, 300), (16, 256, 200), (4, 0, 150),
                                                                 (6, 36, 100)]))
 def test_produce_sweep_vs_reference_kernel(muca, orc, refgpu, L, therm, nup, kernel):
-    if refgpu is None:
-        pytest.skip("reference cubins not present in this checkout")
     rng = np.random.default_rng(L * 3 + 1)
     N = L * L
     lnw = _weights(N, rng)

@@ -1,9 +1,11 @@
 """muca_observables_noalloc: the reweighting sums over caller-owned device
 buffers, with a static scratch array instead of any allocation.  Checked
-against muca_compute_observables (the context path, same kernels) on two
-calls in a row.  This file is collected last, so that in a full run the first
-call of the no-allocation path comes after the other tests' use of the
-library."""
+against muca_compute_observables (the context path, same kernels) and
+against the oracle's restatement of the reference's observables
+(produce2_multigpu.cu:498-518) on two calls in a row, and the device's free
+memory is checked to stay the same across warm calls.  This file is
+collected last, so that in a full run the first call of the no-allocation
+path comes after the other tests' use of the library."""
 import numpy as np
 import pytest
 
@@ -46,7 +48,7 @@ def test_noalloc_rejects_bad_arguments():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("L", [8, 16, 64])
-def test_noalloc_matches_context_path_two_calls(muca, L):
+def test_noalloc_matches_context_path_two_calls(muca, orc, L):
     import torch
     beta = 2.0
     cases = [(_inputs(L, 3 * L), 1.5), (_inputs(L, 3 * L + 1), 1.99)]
@@ -65,9 +67,41 @@ def test_noalloc_matches_context_path_two_calls(muca, L):
     torch.cuda.synchronize()
     for out, exp in zip(outs, expected):
         np.testing.assert_allclose(out.cpu().numpy(), exp, rtol=1e-13, atol=0)
+    # the oracle (the reference's long-double sums) on the same shifted weights
+    N = L * L
+    for ((h, _), delta), (_, wd), out in zip(cases, dev, outs):
+        bz = np.zeros(N + 1)
+        orc.lib().orc_boltz(beta, delta, N, wd.cpu().numpy().copy(), bz, 0)
+        o = orc.observables(beta, N, h, bz)
+        np.testing.assert_allclose(out.cpu().numpy(), o[3:], rtol=1e-12, atol=0)
     # the same input again gives the same sums (no state carried between calls)
     (hd, wd), (_, delta) = dev[0], cases[0]
     again = torch.full((4,), float("nan"), dtype=torch.float64, device="cuda")
     muca.observables_noalloc(0, hd.data_ptr(), wd.data_ptr(), L, beta, delta, again.data_ptr(), stream)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(again.cpu().numpy(), outs[0].cpu().numpy())
+
+
+@pytest.mark.gpu
+def test_noalloc_leaves_free_memory_unchanged(muca):
+    """The defining property: after a first call (which may load the module
+    and looks up the scratch address) further calls change the device's free
+    memory (cudaMemGetInfo) by nothing, and leave the current device alone."""
+    import torch
+    L, beta = 32, 2.0
+    h, lnw = _inputs(L, 11)
+    hd = torch.from_numpy(h.view(np.int64)).cuda()
+    wd = torch.from_numpy(lnw).cuda()
+    out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    muca.observables_noalloc(0, hd.data_ptr(), wd.data_ptr(), L, beta, 1.9, out.data_ptr(), stream)
+    torch.cuda.synchronize()
+    first = out.cpu().numpy().copy()
+    free0, _ = torch.cuda.mem_get_info()
+    for k in range(3):
+        muca.observables_noalloc(0, hd.data_ptr(), wd.data_ptr(), L, beta, 1.9, out.data_ptr(), stream)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, "free device memory moved by %d bytes" % (free0 - free1)
+    assert torch.cuda.current_device() == 0
+    np.testing.assert_array_equal(out.cpu().numpy(), first)
