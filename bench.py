@@ -69,9 +69,12 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ref-gpu", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the flat-run, batch and production lines")
-    p.add_argument("--only", choices=["flat_run", "batch", "production", "random_site"],
+    p.add_argument("--only", choices=["flat_run", "config2", "batch", "production", "random_site"],
                    help="run only this extra line and print it (for profiling a smaller case)")
     p.add_argument("--production-L", type=int, default=128, help="lattice size of --only production")
+    p.add_argument("--blocks", type=int, default=10, help="jackknife blocks of --only production")
+    p.add_argument("--block-sweeps", type=int, default=100, help="production sweeps per block of --only production")
+    p.add_argument("--therm-sweeps", type=int, default=100, help="thermalisation sweeps of --only production")
     p.add_argument("--kernel", type=int, default=0, help="sweep kernel: 0 auto, 1 generic, 2 windowed, 3 specialised")
     return p.parse_args()
 
@@ -374,8 +377,8 @@ def ours_arm(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_ref_gpu:
         out["ref_gpu_kernel"] = ref_gpu_kernel_rate(L, chains)
     if rank == 0 and ws == 1 and not args.no_extra:
-        for key, fn in (("flat_run", flat_run_metric), ("batch", batch_metric), ("production", production_metric),
-                        ("random_site", random_site_metric)):
+        for key, fn in (("flat_run", flat_run_metric), ("config2", config2_metric), ("batch", batch_metric),
+                        ("production", production_metric), ("random_site", random_site_metric)):
             try:
                 out[key] = fn(local)
             except Exception as ex:  # an extra line never fails the bench
@@ -413,6 +416,93 @@ def flat_run_metric(local):
             "init": "Philox4x32-10, key 2024, counter = chain id",
             "loop": "32 iterations (clear, sweep, update) per CUDA-graph replay; device_s = CUDA events "
                     "around the replays, wall_s = host clock of the whole run"}
+
+
+def config2_metric(local, steps=10):
+    """The L=72 configuration as written: runs from starting_M = 1 with
+    NUPDATES doubling every iteration (cap 2^20), with the trivial update and
+    with recursive_update = 1 (the reference's weight_recursion,
+    muca_delta_multigpu.cu:833-859), to min/mean >= 0.5; then the headline
+    step (sweep therm N + nup N, then the update) timed from the converged
+    weights, with each update rule, and each update alone; and the sweep at
+    the reference's own chain count (maxThreadsPerSM * SMs).  L2 is flushed
+    before every timed step."""
+    import numpy as np
+    import torch
+    import muca_gb300 as m
+    L, nc = 72, 16384
+    N = L * L
+    out = {"L": L, "chains": nc}
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    runs = {}
+    w_conv = None
+    for key, rule, max_iter in (("flat_run_trivial", m.UPDATE_TRIVIAL, 3000), ("flat_run_recursion",
+                                                                           m.UPDATE_RECURSION, 400)):
+        with m.Engine(L, nchains=nc, device=local, stream=stream.cuda_stream) as e:
+            res, _ = e.weight_run(starting_M=1, rule=rule, nup_schedule=2, flat_minmean=1, max_iter=max_iter,
+                                  nup_max=1 << 20, records=1, graph_iters=16)
+            if rule == m.UPDATE_TRIVIAL:
+                w_conv = e.get_weights()
+            h = e.histogram()
+        runs[key] = {"iterations": res.iterations, "converged": bool(res.converged),
+                     "width_reached_iteration": res.width_reached_iter, "device_s": res.total_kernel_s,
+                     "wall_s": res.wall_s, "attempts": int(res.total_run + res.iterations * N * nc),
+                     "final_min_over_mean": float(h.min() / max(h.mean(), 1e-300))}
+    out.update(runs)
+    out["schedule"] = "starting_M = 1, NUPDATES doubling every iteration (cap 2^20); stop at min/mean >= 0.5"
+    # the headline step from the converged weights, each update rule
+    steps_out = {}
+    with m.Engine(L, nchains=nc, device=local, stream=stream.cuda_stream) as e:
+        e.init_chains(m.INIT_WEIGHT, 0)
+        for key, rule in (("trivial", m.UPDATE_TRIVIAL), ("recursion", m.UPDATE_RECURSION)):
+            e.set_weights(w_conv)
+            k = 0
+            for _ in range(3):
+                e.sweep(k, 100, 1000, N, N)
+                e.update_weights(rule, wait=False)
+                k += 1
+            ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+            for i in range(steps):
+                e.set_weights(w_conv)  # every timed step starts from the converged weights
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                a, b, c = ev[i]
+                a.record(stream)
+                e.sweep(k, 100, 1000, N, N)
+                b.record(stream)
+                e.update_weights(rule, wait=False)
+                c.record(stream)
+                k += 1
+            torch.cuda.synchronize()
+            step_ms = [x[0].elapsed_time(x[2]) for x in ev]
+            upd_ms = [x[1].elapsed_time(x[2]) for x in ev]
+            steps_out[key] = {"value": 2 * N * nc * steps / (sum(step_ms) * 1e6), "unit": "attempts/ns",
+                              "ms_per_step": sum(step_ms) / steps, "update_us": 1e3 * statistics.median(upd_ms),
+                              "update_share": sum(upd_ms) / sum(step_ms)}
+    out["steps_from_converged_weights"] = steps_out
+    # the sweep at the reference's own chain count
+    nd = m.default_chains(local)
+    with m.Engine(L, nchains=nd, device=local, stream=stream.cuda_stream) as e:
+        e.init_chains(m.INIT_WEIGHT, 0)
+        e.set_weights(w_conv)
+        e.sweep(0, 100, 1000, N, N)
+        best = None
+        for k in range(3):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            e.sweep(k + 1, 100, 1000, N, N)
+            b.record(stream)
+            b.synchronize()
+            t = a.elapsed_time(b)
+            best = t if best is None else min(best, t)
+        out["reference_default_chains"] = {"chains": nd, "value": nd * 2 * N / (best * 1e6), "unit": "attempts/ns",
+                                           "ms": best, "lattice_in_smem": bool(e.info.lattice_in_smem),
+                                           "chains_per_block": e.info.chains_per_block,
+                                           "timing": "best of 3 sweeps (therm N + nup N), converged weights"}
+    return out
 
 
 def batch_metric(local, iters=32):
@@ -502,37 +592,123 @@ def random_site_metric(local, L=72, nc=16384):
     return out
 
 
-def production_metric(local, L=128, with_ref=True, kernel=0):
-    """Production at L=128, 16384 chains (the L=128 configuration's shapes,
-    with the sweep counts scaled down): FP64 weights, 2D (E_Delta, M) u64
-    histogram of 134 M bins; then the reweighting of that histogram."""
+def converge_weight(L, local, nc=16384, stream=None):
+    """A converged weight of the L=72 configuration's kind at size L: the
+    trivial update from zero weights, therm = N and NUPDATES = N doubling
+    once the width is N (cap 2^20), Philox4x32-10 initial spins (key 2024,
+    counter = chain id), until min/mean >= 0.5; 32 iterations per CUDA-graph
+    replay.  Returns (weights, summary)."""
+    import muca_gb300 as m
+    N = L * L
+    with m.Engine(L, nchains=nc, device=local, stream=stream) as e:
+        res, _ = e.weight_run(starting_M=N, rule=m.UPDATE_TRIVIAL, nup_schedule=1, flat_minmean=1, max_iter=20000,
+                              nup_max=1 << 20, init_scheme=m.INIT_CHAIN_COUNTER, records=1, graph_iters=32)
+        w = e.get_weights()
+    return w, {"L": L, "chains": nc, "iterations": res.iterations, "converged": bool(res.converged),
+               "width_reached_iteration": res.width_reached_iter, "device_s": res.total_kernel_s,
+               "wall_s": res.wall_s, "lnW_range": float(w.max() - w.min())}
+
+
+def cpu_produce_rate(L, lnw, nthreads, min_seconds=10.0):
+    """The reference CPU production algorithm (produce.cpp mcs, restated and
+    pinned in the oracle) with one chain per host thread, as produce_mpi runs
+    one chain per rank: production sweeps from the given weight, repeated
+    until about min_seconds of wall time; returns (attempts/ns, sample)."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import orc
+    Lb = orc.lib()
+    N = L * L
+    lnw = np.ascontiguousarray(lnw, np.float64)
+    lats, st, hists = [], [], []
+    for r in range(nthreads):
+        lat = orc.init_lattice(L, 1, Lb.orc_scheme_produce_cpu(0), chain0=r).reshape(-1).copy()
+        ej, ed, mg = (np.array([v[0]], np.int32) for v in orc.energies(L, lat[None, :]))
+        lats.append(lat)
+        st.append((ej, ed, mg))
+        hists.append(np.zeros((N + 1) * (N + 2) // 2, np.uint64))  # lazily mapped; one per rank
+
+    def run(r, k, sweeps):
+        ej, ed, mg = st[r]
+        Lb.orc_produce_cpu_mcs(L, r, lats[r], ej, ed, mg, lnw, hists[r], 0, k, 0, sweeps * N)
+
+    done, t_total, k, sweeps = 0, 0.0, 0, 1
+    with ThreadPoolExecutor(nthreads) as ex:
+        while t_total < min_seconds:
+            t0 = time.perf_counter()
+            list(ex.map(lambda r: run(r, k, sweeps), range(nthreads)))
+            dt = time.perf_counter() - t0
+            t_total += dt
+            done += nthreads * sweeps * N
+            k += 1
+            sweeps = max(1, min(64, int(sweeps * 2 if dt < 2.0 else sweeps)))
+    return done / (t_total * 1e9), ("%d chains (one per host thread), %d production sweeps each at L=%d from the "
+                                    "converged weight, %.1f s wall" % (nthreads, done // (nthreads * N), L, t_total))
+
+
+def production_metric(local, L=128, with_ref=True, kernel=0, blocks=10, therm_sweeps=100, block_sweeps=100,
+                      with_cpu=True):
+    """The L=128 production configuration with its shapes and scaled sweep
+    counts: a converged L=128 weight (converge_weight), 16384 chains from the
+    reference production initialisation, `therm_sweeps` thermalisation
+    sweeps, then `blocks` jackknife blocks of `block_sweeps` production
+    sweeps each (the JACKS blocks of produce.cpp:201-247; seeds of the
+    reference's block loop, produce2_multigpu.cu:324-347), every block's 2D
+    (E_Delta, M) histogram reweighted at Delta = 1.96 (produce2_multigpu.cu:
+    293-300,498-518) into <|M|>, chi and U4, jackknifed over the blocks.
+    The configuration asks for 10^5 thermalisation and 10^7 production sweeps;
+    the run scales them by therm_sweeps / 10^5 and blocks * block_sweeps / 10^7."""
     import numpy as np
     import torch
     import muca_gb300 as m
     nc = 16384
     N = L * L
+    beta, delta = 2.0, 1.96
     stream = torch.cuda.Stream()
+    w, wsum = converge_weight(L, local, nc, stream.cuda_stream)
+    per_block = []
     with m.Engine(L, nchains=nc, device=local, mode=m.MODE_PRODUCE, stream=stream.cuda_stream, kernel=kernel) as e:
         e.init_chains(m.INIT_PRODUCE, 0)
-        e.set_weights(np.zeros(N + 1))
-        e.sweep(0, 100, 1000, N, 0)  # one thermalisation sweep
-        sweeps = 4
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        e.sweep(1, 100, 2000, 0, sweeps * N)
-        e1.record(stream)
-        e1.synchronize()
-        t_sweep = e0.elapsed_time(e1) * 1e-3
-        e.weight_shift(2.0, 1.96)
-        e.observables(2.0, 1.96)
-        t0 = time.perf_counter()
-        reps = 5
-        for _ in range(reps):
-            e.observables(2.0, 1.96)
-        t_obs = (time.perf_counter() - t0) / reps
+        e.set_weights(w)
+        e.weight_shift(beta, delta)  # the reweighting copy only; the sweep keeps w
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        e.sweep(0, 100, 1000, therm_sweeps * N, 0)  # thermalisation: iter 0, seed SEED+1000*GPU+l (l = 0)
+        a1.record(stream)
+        sweep_ms, obs_ms = [], []
+        for jj in range(blocks):
+            b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            b0.record(stream)
+            e.sweep(jj, 100, 2000, 0, block_sweeps * N)  # block jj: iter jj, seed SEED+2000*GPU+l
+            b1.record(stream)
+            t0 = time.perf_counter()
+            o = e.observables(beta, delta)  # launch, reweighting kernels, read-back
+            obs_ms.append(1e3 * (time.perf_counter() - t0))
+            per_block.append((o.m_abs, o.chi, o.u4))
+            sweep_ms.append(b0.elapsed_time(b1))
+        torch.cuda.synchronize()
+        therm_ms = a0.elapsed_time(a1)
+        info = e.info
+        jk = [e.jackknife(np.array([pb[i] for pb in per_block])) for i in range(3)]
+    att = nc * block_sweeps * N * blocks
     bins = (N + 1) * (N + 2) // 2
+    out = {"metric": "production sweep attempts/ns at L=%d" % L, "value": att / (sum(sweep_ms) * 1e6),
+           "unit": "attempts/ns", "chains": nc, "kernel": info.kernel, "lattice_in_smem": info.lattice_in_smem,
+           "weight": wsum,
+           "therm": {"sweeps": therm_sweeps, "ms": therm_ms,
+                     "value": nc * therm_sweeps * N / (therm_ms * 1e6)},
+           "blocks": blocks, "block_sweeps": block_sweeps,
+           "scale": {"therm": therm_sweeps / 1e5, "production": blocks * block_sweeps / 1e7},
+           "observables": {"delta": delta, "beta": beta,
+                           "m_abs": {"value": jk[0][0], "jackknife_error": jk[0][1]},
+                           "chi": {"value": jk[1][0], "jackknife_error": jk[1][1]},
+                           "u4": {"value": jk[2][0], "jackknife_error": jk[2][1]},
+                           "per_block": [list(pb) for pb in per_block]},
+           "timing": "CUDA events around each block's production launch",
+           "reweighting": {"bins": bins, "ms": statistics.median(obs_ms), "GB_per_s": 8 * bins / statistics.median(
+               obs_ms) / 1e6, "timing": "host clock per block (launch, two kernels, read-back of 4 sums), median"}}
     ref = None
-    try:  # the reference production kernel on the same lattice and step
+    try:  # the reference production kernel on the same lattice, weights and step
         if not with_ref:
             raise RuntimeError("not requested")
         from oracle import orc
@@ -542,18 +718,19 @@ def production_metric(local, L=128, with_ref=True, kernel=0):
                 e2.init_chains(m.INIT_PRODUCE, 0)
                 lat0 = e2.get_lattice()
             z = np.zeros(nc, np.int32)
-            w64 = np.zeros(N + 1)
-            lat1, _, ej, ed, mg, _ = orc.refgpu_produce(L, lat0, w64, z, z, z, 0, 100, N, 0, compute_energies=True)
-            _, _, _, _, _, ms = orc.refgpu_produce(L, lat1, w64, ej, ed, mg, 1, 100, 0, sweeps * N)
-            ref = {"value": nc * sweeps * N / (ms * 1e6), "ms": ms,
-                   "kernel": "produce2_multigpu.cu mcs, compiled for sm_103a, same lattice, weights and step"}
-    except Exception as ex:
+            lat1, _, ej, ed, mg, _ = orc.refgpu_produce(L, lat0, w, z, z, z, 0, 100, N, 0, compute_energies=True)
+            _, _, _, _, _, ms = orc.refgpu_produce(L, lat1, w, ej, ed, mg, 1, 100, 0, 4 * N)
+            ref = {"value": nc * 4 * N / (ms * 1e6), "ms": ms, "sweeps": 4,
+                   "kernel": "produce2_multigpu.cu mcs, compiled for sm_103a, same lattice and converged weights"}
+    except Exception as ex:  # noqa: BLE001
         ref = {"unavailable": str(ex)[:200]}
-    return {"metric": "production sweep attempts/ns at L=%d" % L, "value": nc * sweeps * N / (t_sweep * 1e9),
-            "ref_gpu_kernel": ref,
-            "unit": "attempts/ns", "chains": nc, "sweeps": sweeps, "timing": "CUDA events around one launch",
-            "reweighting": {"bins": bins, "ms": 1e3 * t_obs, "GB_per_s": 8 * bins / t_obs / 1e9,
-                            "timing": "host clock, mean of %d calls (histogram read once per call)" % reps}}
+    out["ref_gpu_kernel"] = ref
+    if with_cpu:
+        nthreads = os.cpu_count() or 1
+        v, sample = cpu_produce_rate(L, w, nthreads)
+        out["cpu_baseline"] = {"value": v, "unit": "attempts/ns", "cores": nthreads, "kind": "port",
+                               "sample": sample}
+    return out
 
 
 def ref_gpu_kernel_rate(L, chains):
@@ -596,8 +773,12 @@ def main():
         torch.cuda.set_device(local)
         from muca_gb300 import build as b
         b.build()
-        fn = {"flat_run": flat_run_metric, "batch": batch_metric, "random_site": random_site_metric,
-              "production": lambda d: production_metric(d, args.production_L, with_ref=False, kernel=args.kernel)}[args.only]
+        fn = {"flat_run": flat_run_metric, "config2": config2_metric, "batch": batch_metric,
+              "random_site": random_site_metric,
+              "production": lambda d: production_metric(d, args.production_L, with_ref=False, kernel=args.kernel,
+                                                        blocks=args.blocks, block_sweeps=args.block_sweeps,
+                                                        therm_sweeps=args.therm_sweeps,
+                                                        with_cpu=not args.no_cpu_baseline)}[args.only]
         print(json.dumps(fn(local)))
         return 0
     return ours_arm(args, ws, rank, local)

@@ -61,6 +61,87 @@ struct AddD {
     __device__ static double id() { return 0.0; }
 };
 
+// The prefix of weight_recursion (muca_delta_multigpu.cu:848-858) over the
+// pairs i in [start, end):  x_start = lnW[start],
+//   x_{i+1} = x_i + dS_i  if pair i is connected (valid[i]),  else lnW[i+1]
+// (a pair with an empty bin leaves lnW[i+1] as it was).  The reference runs
+// it as one dependent chain of FP64 additions; here the block of (whole
+// warps of) threads splits [start, end) into contiguous chunks, each thread
+// composes its chunk's maps x -> x + d / x -> c into one, the block scans
+// those compositions (warp shuffles, then the warp totals), and every thread
+// replays its chunk from its prefix.  Inside a chunk the additions keep the
+// reference's order; across chunks they are grouped by the tree, which moves
+// the result by a few units in the last place of the partial sums.
+// `inc` holds dS_i and `cval` lnW[i+1] of the pairs; out[i] gets x_{i+1}.
+// Must be called by every thread of the block.
+struct SegMap {
+    double t;  // valid: the added sum; not valid: the constant
+    int v;     // 1: x -> x + t, 0: x -> t
+};
+__device__ __forceinline__ SegMap seg_then(SegMap first, SegMap then)
+{
+    SegMap r;
+    r.v = first.v & then.v;
+    r.t = then.v ? __dadd_rn(first.t, then.t) : then.t;
+    return r;
+}
+
+__device__ void block_segmented_prefix(int start, int end, double x0, const double *__restrict__ inc,
+                                       const unsigned char *__restrict__ valid,
+                                       const double *__restrict__ cval, double *__restrict__ out)
+{
+    __shared__ double s_t[32];
+    __shared__ int s_v[32];
+    const int n = end - start;
+    if (n <= 0) return;
+    const int nt = (int)blockDim.x, tid = (int)threadIdx.x;
+    const int chunk = (n + nt - 1) / nt;
+    const int lo = start + tid * chunk, hi = min(lo + chunk, end);
+    SegMap a{0.0, 1};
+    for (int i = lo; i < hi; ++i) {
+        const SegMap e{valid[i] ? inc[i] : cval[i], valid[i] ? 1 : 0};
+        a = seg_then(a, e);
+    }
+    // inclusive scan of the thread maps within the warp
+    const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+    SegMap sc = a;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        SegMap pr;
+        pr.t = __shfl_up_sync(0xffffffffu, sc.t, o);
+        pr.v = __shfl_up_sync(0xffffffffu, sc.v, o);
+        if (lane >= o) sc = seg_then(pr, sc);
+    }
+    if (lane == 31) { s_t[wid] = sc.t; s_v[wid] = sc.v; }
+    __syncthreads();
+    if (wid == 0) {
+        SegMap w{lane < nw ? s_t[lane] : 0.0, lane < nw ? s_v[lane] : 1};
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            SegMap pr;
+            pr.t = __shfl_up_sync(0xffffffffu, w.t, o);
+            pr.v = __shfl_up_sync(0xffffffffu, w.v, o);
+            if (lane >= o) w = seg_then(pr, w);
+        }
+        s_t[lane] = w.t;
+        s_v[lane] = w.v;
+    }
+    __syncthreads();
+    // exclusive prefix of this thread: the warps before it, then the lanes before it
+    SegMap ex{0.0, 1};
+    if (wid > 0) ex = SegMap{s_t[wid - 1], s_v[wid - 1]};
+    SegMap lp;
+    lp.t = __shfl_up_sync(0xffffffffu, sc.t, 1);
+    lp.v = __shfl_up_sync(0xffffffffu, sc.v, 1);
+    if (lane > 0) ex = seg_then(ex, lp);
+    double x = ex.v ? __dadd_rn(x0, ex.t) : ex.t;
+    for (int i = lo; i < hi; ++i) {
+        x = valid[i] ? __dadd_rn(x, inc[i]) : cval[i];
+        out[i] = x;
+    }
+    __syncthreads();
+}
+
 // Statistics of hist[0..N], then (if the update is due) the weight update.
 // ctl == nullptr: standalone call, update iff rule >= 0.
 // ctl != nullptr: one iteration of a device-driven run (see RunCtl).
@@ -141,6 +222,27 @@ __device__ __forceinline__ int bookkeep(int start, int end, unsigned long long v
     return upd;
 }
 
+// Pair i of weight_recursion (muca_delta_multigpu.cu:850-856): for i in
+// [start, end) with H_i, H_{i+1} both nonzero,
+//   p = H_i H_{i+1} / (H_i + H_{i+1}),  k = p / (p + p_acc[i]),
+//   dS_i = (lnW[i+1] - lnW[i]) + k ln(H_i / H_{i+1}),  p_acc[i] += p;
+// returns whether the pair is connected (ds[i] written).
+__device__ __forceinline__ unsigned char recursion_increment(const unsigned long long *__restrict__ hist,
+                                                             const double *__restrict__ lnw,
+                                                             double *__restrict__ p_acc, uint32_t i, int start,
+                                                             int end, double *__restrict__ ds)
+{
+    if ((int)i < start || (int)i >= end) return 0;
+    const unsigned long long a = hist[i], b = hist[i + 1];
+    if ((a == 0) | (b == 0)) return 0;
+    const double p = __ddiv_rn((double)(a * b), (double)(a + b));
+    const double k = __ddiv_rn(p, __dadd_rn(p, p_acc[i]));
+    const double lg = log(__ddiv_rn((double)a, (double)b));
+    ds[i] = __dadd_rn(__dadd_rn(-lnw[i], lnw[i + 1]), __dmul_rn(k, lg));
+    p_acc[i] = __dadd_rn(p_acc[i], p);
+    return 1;
+}
+
 // `dyn`: dynamic shared memory of update_smem(N, rule) bytes.
 __device__ __forceinline__ void weight_update_body(const unsigned long long *__restrict__ hist, uint32_t N,
                                                    double *__restrict__ lnw, float *__restrict__ w32,
@@ -210,33 +312,11 @@ __device__ __forceinline__ void weight_update_body(const unsigned long long *__r
     // (a) the increments dS_i of all connected pairs, in parallel;
     double *ds = reinterpret_cast<double *>(dyn);
     unsigned char *valid = dyn + sizeof(double) * (size_t)N;
-    for (uint32_t i = tid; i < N; i += bs) {
-        unsigned char ok = 0;
-        if ((int)i >= start && (int)i < end) {
-            const unsigned long long a = hist[i], b = hist[i + 1];
-            if ((a != 0) & (b != 0)) {
-                const double p = __ddiv_rn((double)(a * b), (double)(a + b));
-                const double k = __ddiv_rn(p, __dadd_rn(p, p_acc[i]));
-                const double lg = log(__ddiv_rn((double)a, (double)b));
-                ds[i] = __dadd_rn(__dadd_rn(-lnw[i], lnw[i + 1]), __dmul_rn(k, lg));
-                p_acc[i] = __dadd_rn(p_acc[i], p);
-                ok = 1;
-            }
-        }
-        valid[i] = ok;
-    }
+    for (uint32_t i = tid; i < N; i += bs) valid[i] = recursion_increment(hist, lnw, p_acc, i, start, end, ds);
     __syncthreads();
-    // (b) the prefix lnW[i+1] = lnW[i] + dS_i, sequential as in the reference
-    //     (a pair with an empty bin leaves lnW[i+1] at its old value);
-    if (tid == 0) {
-        double cur = lnw[start];
-        for (int i = start; i < end; ++i) {
-            const double nxt = valid[i] ? __dadd_rn(cur, ds[i]) : lnw[i + 1];
-            ds[i] = nxt;
-            cur = nxt;
-        }
-    }
-    __syncthreads();
+    // (b) the prefix lnW[i+1] = lnW[i] + dS_i, in place over ds (a pair
+    //     with an empty bin leaves lnW[i+1] at its old value);
+    block_segmented_prefix(start, end, lnw[start], ds, valid, lnw + 1, ds);
     // (c) write back and normalise by lnW[0] (bin 0 is never rewritten)
     for (uint32_t i = tid; i <= N; i += bs) {
         double v = ((int)i > start && (int)i <= end) ? ds[i - 1] : lnw[i];
@@ -368,6 +448,8 @@ __global__ void __launch_bounds__(kUpdMultiThreads) k_upd_kl(const unsigned long
     int start = lo, end = hi < 0 ? 0 : hi;
     if (start > end) { start = 0; end = 0; }
     sc->upd = bookkeep(start, end, vis, ev, mn, klt, N, rule, stats, ctl);
+    sc->start = start;
+    sc->end = end;
     // lnW[0] after its ln H subtraction (:469), from the weights before any write
     const unsigned long long h0 = hist[0], thr = rule == 0 ? 1ull : 0ull;
     sc->tmp = h0 > thr ? __dsub_rn(lnw[0], log((double)h0)) : lnw[0];
@@ -392,12 +474,49 @@ __global__ void __launch_bounds__(kUpdMultiThreads) k_upd_apply(const unsigned l
     }
 }
 
+// Rule 2 over kUpdBlocks blocks: the increments of every connected pair
+// (FP64 divisions and a logarithm each) ...
+__global__ void __launch_bounds__(kUpdMultiThreads) k_upd_rec_inc(const unsigned long long *__restrict__ hist,
+                                                                  uint32_t N, const double *__restrict__ lnw,
+                                                                  double *__restrict__ p_acc,
+                                                                  const UpdScratch *__restrict__ sc, RecScratch rs)
+{
+    if (!sc->upd) return;
+    const int start = sc->start, end = sc->end;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+        rs.valid[i] = recursion_increment(hist, lnw, p_acc, i, start, end, rs.ds);
+}
+
+// ... then the prefix as one block's segmented scan, the write-back and the
+// normalisation by lnW[0] (bin 0 is never rewritten by the recursion).
+__global__ void __launch_bounds__(kUpdThreads) k_upd_rec_scan(uint32_t N, double *__restrict__ lnw,
+                                                               float *__restrict__ w32,
+                                                               const UpdScratch *__restrict__ sc, RecScratch rs)
+{
+    if (!sc->upd) return;
+    const int start = sc->start, end = sc->end;
+    const double lnw0 = lnw[0];
+    block_segmented_prefix(start, end, lnw[start], rs.ds, rs.valid, lnw + 1, rs.ds);
+    for (uint32_t i = threadIdx.x; i <= N; i += blockDim.x) {
+        double v = ((int)i > start && (int)i <= end) ? rs.ds[i - 1] : lnw[i];
+        v = __dsub_rn(v, lnw0);
+        lnw[i] = v;
+        w32[i] = (float)v;
+    }
+}
+
 static cudaError_t launch_update_multi(const unsigned long long *hist, uint32_t N, double *lnw, float *w32,
-                                       int rule, HistStatsDev *stats, RunCtl *ctl, UpdScratch *sc, cudaStream_t s)
+                                       double *p_acc, int rule, HistStatsDev *stats, RunCtl *ctl, UpdScratch *sc,
+                                       const RecScratch *rs, cudaStream_t s)
 {
     k_upd_stats<<<kUpdBlocks, kUpdMultiThreads, 0, s>>>(hist, N, ctl, sc);
     k_upd_kl<<<kUpdBlocks, kUpdMultiThreads, 0, s>>>(hist, N, lnw, rule, stats, ctl, sc);
-    if (rule >= 0) k_upd_apply<<<kUpdBlocks, kUpdMultiThreads, 0, s>>>(hist, N, lnw, w32, rule, sc);
+    if (rule == 2) {
+        k_upd_rec_inc<<<kUpdBlocks, kUpdMultiThreads, 0, s>>>(hist, N, lnw, p_acc, sc, *rs);
+        k_upd_rec_scan<<<1, kUpdThreads, 0, s>>>(N, lnw, w32, sc, *rs);
+    } else if (rule >= 0) {
+        k_upd_apply<<<kUpdBlocks, kUpdMultiThreads, 0, s>>>(hist, N, lnw, w32, rule, sc);
+    }
     return cudaGetLastError();
 }
 
@@ -434,9 +553,9 @@ static cudaError_t prep_update(uint32_t N, int rule)
 }
 
 cudaError_t launch_weight_update(const unsigned long long *hist, uint32_t N, double *lnw, float *w32, double *p_acc,
-                                 int rule, HistStatsDev *stats, cudaStream_t s, UpdScratch *sc)
+                                 int rule, HistStatsDev *stats, cudaStream_t s, UpdScratch *sc, const RecScratch *rs)
 {
-    if (sc && rule != 2) return launch_update_multi(hist, N, lnw, w32, rule, stats, nullptr, sc, s);
+    if (sc && (rule != 2 || rs)) return launch_update_multi(hist, N, lnw, w32, p_acc, rule, stats, nullptr, sc, rs, s);
     cudaError_t e = prep_update(N, rule);
     if (e != cudaSuccess) return e;
     k_weight_update<<<1, kUpdThreads, update_smem(N, rule), s>>>(hist, N, lnw, w32, p_acc, rule, stats, nullptr);
@@ -444,9 +563,9 @@ cudaError_t launch_weight_update(const unsigned long long *hist, uint32_t N, dou
 }
 
 cudaError_t launch_run_update(const unsigned long long *hist, double *lnw, float *w32, double *p_acc, RunCtl *ctl,
-                              cudaStream_t s, uint32_t N, int rule, UpdScratch *sc)
+                              cudaStream_t s, uint32_t N, int rule, UpdScratch *sc, const RecScratch *rs)
 {
-    if (sc && rule != 2) return launch_update_multi(hist, N, lnw, w32, rule, nullptr, ctl, sc, s);
+    if (sc && (rule != 2 || rs)) return launch_update_multi(hist, N, lnw, w32, p_acc, rule, nullptr, ctl, sc, rs, s);
     cudaError_t e = prep_update(N, rule);
     if (e != cudaSuccess) return e;
     k_weight_update<<<1, kUpdThreads, update_smem(N, rule), s>>>(hist, N, lnw, w32, p_acc, rule, nullptr, ctl);

@@ -49,6 +49,7 @@ struct muca_ctx {
     double log_eps = 0, log_eps_measured = 0;
     uint32_t algo = 0;
     float *d_logf_tab = nullptr;  // random-site algorithm with host_logf: the host libm's logf
+    RecScratch rec{};             // the multi-block recursion's dS_i and pair flags (weight mode)
     long long wait_cycles = 0;    // bound of the sweep's device-side waits (0 = default)
     uint32_t hooks = 0;           // test hooks of the sweep (kHook*)
     std::string err;
@@ -87,7 +88,7 @@ void free_all(muca_ctx *c)
 {
     void *dp[] = {c->d_lat, c->d_ej, c->d_edel, c->d_mag, c->d_lnw, c->d_lnw_obs, c->d_pacc, c->d_w32, c->d_hist,
                   c->d_index, c->d_naver, c->d_stats, c->d_ctl, c->d_recs, c->d_obs_part, c->d_obs_out,
-                  c->d_jk, c->d_tmp, c->d_bad, c->d_err, c->d_logf_tab, c->d_upd};
+                  c->d_jk, c->d_tmp, c->d_bad, c->d_err, c->d_logf_tab, c->d_upd, c->rec.ds, c->rec.valid};
     for (void *p : dp)
         if (p) cudaFree(p);
     void *hp[] = {c->h_stats, c->h_ctl, c->h_obs_out, c->h_bad, c->h_err};
@@ -306,6 +307,10 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
     CREATE_TRY(dmalloc(c, &c->d_stats, 1));
     CREATE_TRY(dmalloc(c, &c->d_upd, 1));
     CREATE_TRY(cudaMemsetAsync(c->d_upd, 0, sizeof(UpdScratch), c->stream));
+    if (c->mode == MUCA_MODE_WEIGHT) {
+        CREATE_TRY(dmalloc(c, &c->rec.ds, (size_t)N));
+        CREATE_TRY(dmalloc(c, &c->rec.valid, (size_t)N));
+    }
     CREATE_TRY(dmalloc(c, &c->d_ctl, 1));
     CREATE_TRY(dmalloc(c, &c->d_bad, 1));
     CREATE_TRY(dmalloc(c, &c->d_err, 1));
@@ -591,7 +596,8 @@ static muca_status update_impl(muca_ctx *c, int rule, muca_hist_stats *st)
     if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
     if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "weight statistics need a weight-mode context");
     CUDA_TRY(c, cudaSetDevice(c->device));
-    CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, rule, c->d_stats, c->stream, c->d_upd));
+    CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, rule, c->d_stats, c->stream, c->d_upd,
+                                     &c->rec));
     if (!st) return MUCA_OK;  // enqueue only
     CUDA_TRY(c, cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(HistStatsDev), cudaMemcpyDeviceToHost, c->stream));
     if (muca_status e = check_err(c)) return e;
@@ -631,7 +637,7 @@ muca_status muca_iterate_host(muca_ctx *c, const double *lnw_in, uint32_t iter, 
     }
     if (muca_status e = do_sweep(c, iter, seed_base, seed_dev_mul, therm, nup, true)) return e;
     CUDA_TRY(c, launch_weight_update(c->d_hist, c->N, c->d_lnw, c->d_w32, c->d_pacc, (int)rule, c->d_stats, c->stream,
-                                     c->d_upd));
+                                     c->d_upd, &c->rec));
     if (st) CUDA_TRY(c, cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(HistStatsDev), cudaMemcpyDeviceToHost, c->stream));
     if (lnw_out) CUDA_TRY(c, cudaMemcpyAsync(lnw_out, c->d_lnw, n * 8, cudaMemcpyDeviceToHost, c->stream));
     if (hist_out) CUDA_TRY(c, cudaMemcpyAsync(hist_out, c->d_hist, n * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -726,7 +732,7 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
                         ? launch_sweep_random(ra, c->plan.cpb, c->plan.blocks, (int)c->rounds, c->smem_optin, c->stream)
                         : launch_sweep(c->plan, a, c->stream);
             if (e == cudaSuccess) e = launch_run_update(c->d_hist, c->d_lnw, c->d_w32, c->d_pacc, c->d_ctl, c->stream,
-                                                        c->N, (int)o->rule, c->d_upd);
+                                                        c->N, (int)o->rule, c->d_upd, &c->rec);
         }
         if (capturing) {
             const cudaError_t ec = cudaStreamEndCapture(c->stream, &graph);
@@ -763,7 +769,7 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
                     : launch_sweep(c->plan, a, c->stream);
         if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
         if (e == cudaSuccess) e = launch_run_update(c->d_hist, c->d_lnw, c->d_w32, c->d_pacc, c->d_ctl, c->stream,
-                                                        c->N, (int)o->rule, c->d_upd);
+                                                        c->N, (int)o->rule, c->d_upd, &c->rec);
         if (e == cudaSuccess) e = cudaEventRecord(m0, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(&h.st, &c->d_ctl->st, sizeof(IterState), cudaMemcpyDeviceToHost, c->stream);
         if (e == cudaSuccess) e = cudaEventRecord(m1, c->stream);

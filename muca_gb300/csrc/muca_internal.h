@@ -141,14 +141,22 @@ struct UpdScratch {
     unsigned int done;
     int upd;
     double tmp;
+    int start, end;  // the histogram's range (bins with H > 1), for the recursion
+};
+// Global scratch of the multi-block recursion: dS_i (N doubles) and the
+// connected-pair flags (N bytes).
+struct RecScratch {
+    double *ds;
+    unsigned char *valid;
 };
 // stats of hist[0..N]; if rule >= 0 also updates lnw (FP64) / w32 (FP32 shadow)
 // (rule: 0 trivial, 1 trivial-cpu, 2 recursion with p_acc).  With `sc`
 // (zero-initialised once) rules -1, 0 and 1 spread their FP64 work over
-// kUpdBlocks blocks; the recursion always runs in one block.
+// kUpdBlocks blocks, and so does rule 2 when `rs` is given too (its prefix
+// then runs as one block's segmented scan); otherwise one block does all.
 cudaError_t launch_weight_update(const unsigned long long *hist, uint32_t N, double *lnw, float *w32,
                                  double *p_acc, int rule, HistStatsDev *stats, cudaStream_t s,
-                                 UpdScratch *sc = nullptr);
+                                 UpdScratch *sc = nullptr, const RecScratch *rs = nullptr);
 
 // Device-resident state of a weight-estimation run (the loop of
 // muca_delta_multigpu.cu:374-477).  The first three words are what the
@@ -217,7 +225,8 @@ cudaError_t launch_batch_update(const BatchInst *insts, uint32_t n_inst, uint32_
 // One iteration's tail: statistics, width/convergence bookkeeping, weight
 // update, schedule of the next NUPDATES; a no-op once st.stop is set.
 cudaError_t launch_run_update(const unsigned long long *hist, double *lnw, float *w32, double *p_acc,
-                              RunCtl *ctl, cudaStream_t s, uint32_t N, int rule, UpdScratch *sc = nullptr);
+                              RunCtl *ctl, cudaStream_t s, uint32_t N, int rule, UpdScratch *sc = nullptr,
+                              const RecScratch *rs = nullptr);
 // Clears the weight histogram unless the run has stopped.
 cudaError_t launch_run_clear(unsigned long long *hist, uint32_t n, const RunCtl *ctl, cudaStream_t s);
 cudaError_t launch_weights_to_f32(const double *lnw, float *w32, uint32_t n, cudaStream_t s);
