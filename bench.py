@@ -437,20 +437,27 @@ def config2_metric(local, steps=10):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     runs = {}
     w_conv = None
-    for key, rule, max_iter in (("flat_run_trivial", m.UPDATE_TRIVIAL, 3000), ("flat_run_recursion",
-                                                                           m.UPDATE_RECURSION, 400)):
+    plans = (("flat_run_reference_schedule", m.UPDATE_TRIVIAL, 0, 0, 20000,
+              "NUPDATES = starting_M = 1 until the width is N, then (NUP + 1) * 1.01 per iteration "
+              "(muca_delta_multigpu.cu:379-382)"),
+             ("flat_run_doubling", m.UPDATE_TRIVIAL, 2, 1 << 14, 20000,
+              "NUPDATES = starting_M = 1 doubling every iteration, capped at 2^14"),
+             ("flat_run_recursion", m.UPDATE_RECURSION, 0, 0, 3000,
+              "recursive_update = 1 (weight_recursion, muca_delta_multigpu.cu:833-859), reference schedule"))
+    for key, rule, sched, cap, max_iter, desc in plans:
         with m.Engine(L, nchains=nc, device=local, stream=stream.cuda_stream) as e:
-            res, _ = e.weight_run(starting_M=1, rule=rule, nup_schedule=2, flat_minmean=1, max_iter=max_iter,
-                                  nup_max=1 << 20, records=1, graph_iters=16)
-            if rule == m.UPDATE_TRIVIAL:
+            res, _ = e.weight_run(starting_M=1, rule=rule, nup_schedule=sched, flat_minmean=1, max_iter=max_iter,
+                                  nup_max=cap, records=1, graph_iters=32)
+            if key == "flat_run_reference_schedule":
                 w_conv = e.get_weights()
             h = e.histogram()
-        runs[key] = {"iterations": res.iterations, "converged": bool(res.converged),
-                     "width_reached_iteration": res.width_reached_iter, "device_s": res.total_kernel_s,
-                     "wall_s": res.wall_s, "attempts": int(res.total_run + res.iterations * N * nc),
+        runs[key] = {"schedule": desc, "iterations": res.iterations, "converged": bool(res.converged),
+                     "width_reached_iteration": None if res.width_reached_iter == 0xFFFFFFFF else res.width_reached_iter,
+                     "device_s": res.total_kernel_s, "wall_s": res.wall_s,
+                     "attempts": int(res.total_run + res.iterations * N * nc),
                      "final_min_over_mean": float(h.min() / max(h.mean(), 1e-300))}
     out.update(runs)
-    out["schedule"] = "starting_M = 1, NUPDATES doubling every iteration (cap 2^20); stop at min/mean >= 0.5"
+    out["stop"] = "min/mean >= 0.5 (iteration cap as given); therm = N per iteration; 32 iterations per graph"
     # the headline step from the converged weights, each update rule
     steps_out = {}
     with m.Engine(L, nchains=nc, device=local, stream=stream.cuda_stream) as e:
@@ -597,16 +604,17 @@ def converge_weight(L, local, nc=16384, stream=None):
     trivial update from zero weights, therm = N and NUPDATES = N doubling
     once the width is N (cap 2^20), Philox4x32-10 initial spins (key 2024,
     counter = chain id), until min/mean >= 0.5; 32 iterations per CUDA-graph
-    replay.  Returns (weights, summary)."""
+    replay.  Returns (weights, the chains' final lattices, summary)."""
     import muca_gb300 as m
     N = L * L
     with m.Engine(L, nchains=nc, device=local, stream=stream) as e:
         res, _ = e.weight_run(starting_M=N, rule=m.UPDATE_TRIVIAL, nup_schedule=1, flat_minmean=1, max_iter=20000,
                               nup_max=1 << 20, init_scheme=m.INIT_CHAIN_COUNTER, records=1, graph_iters=32)
         w = e.get_weights()
-    return w, {"L": L, "chains": nc, "iterations": res.iterations, "converged": bool(res.converged),
-               "width_reached_iteration": res.width_reached_iter, "device_s": res.total_kernel_s,
-               "wall_s": res.wall_s, "lnW_range": float(w.max() - w.min())}
+        lat = e.get_lattice()
+    return w, lat, {"L": L, "chains": nc, "iterations": res.iterations, "converged": bool(res.converged),
+                    "width_reached_iteration": res.width_reached_iter, "device_s": res.total_kernel_s,
+                    "wall_s": res.wall_s, "lnW_range": float(w.max() - w.min())}
 
 
 def cpu_produce_rate(L, lnw, nthreads, min_seconds=10.0):
@@ -657,7 +665,14 @@ def production_metric(local, L=128, with_ref=True, kernel=0, blocks=10, therm_sw
     (E_Delta, M) histogram reweighted at Delta = 1.96 (produce2_multigpu.cu:
     293-300,498-518) into <|M|>, chi and U4, jackknifed over the blocks.
     The configuration asks for 10^5 thermalisation and 10^7 production sweeps;
-    the run scales them by therm_sweeps / 10^5 and blocks * block_sweeps / 10^7."""
+    the run scales them by therm_sweeps / 10^5 and blocks * block_sweeps / 10^7.
+    So few sweeps move a walker only ~10^3 bins along E_Delta (N + 1 =
+    16385 bins), so the chains start from the weight run's final lattices,
+    which the converged multicanonical walk has spread over all of E_Delta,
+    instead of fresh random spins (E_Delta ~ 2N/3 for every chain): from
+    there no block would sample the E_Delta that dominate the reweighting at
+    Delta = 1.96, and every Boltzmann factor of the rows it did sample would
+    underflow."""
     import numpy as np
     import torch
     import muca_gb300 as m
@@ -665,10 +680,11 @@ def production_metric(local, L=128, with_ref=True, kernel=0, blocks=10, therm_sw
     N = L * L
     beta, delta = 2.0, 1.96
     stream = torch.cuda.Stream()
-    w, wsum = converge_weight(L, local, nc, stream.cuda_stream)
+    w, lat_w, wsum = converge_weight(L, local, nc, stream.cuda_stream)
     per_block = []
     with m.Engine(L, nchains=nc, device=local, mode=m.MODE_PRODUCE, stream=stream.cuda_stream, kernel=kernel) as e:
-        e.init_chains(m.INIT_PRODUCE, 0)
+        e.set_lattice(lat_w)  # the equilibrated multicanonical walkers
+        del lat_w
         e.set_weights(w)
         e.weight_shift(beta, delta)  # the reweighting copy only; the sweep keeps w
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -681,6 +697,7 @@ def production_metric(local, L=128, with_ref=True, kernel=0, blocks=10, therm_sw
             b0.record(stream)
             e.sweep(jj, 100, 2000, 0, block_sweeps * N)  # block jj: iter jj, seed SEED+2000*GPU+l
             b1.record(stream)
+            b1.synchronize()
             t0 = time.perf_counter()
             o = e.observables(beta, delta)  # launch, reweighting kernels, read-back
             obs_ms.append(1e3 * (time.perf_counter() - t0))
@@ -697,6 +714,7 @@ def production_metric(local, L=128, with_ref=True, kernel=0, blocks=10, therm_sw
            "weight": wsum,
            "therm": {"sweeps": therm_sweeps, "ms": therm_ms,
                      "value": nc * therm_sweeps * N / (therm_ms * 1e6)},
+           "start": "the weight run's final lattices (spread over E_Delta by the converged walk)",
            "blocks": blocks, "block_sweeps": block_sweeps,
            "scale": {"therm": therm_sweeps / 1e5, "production": blocks * block_sweeps / 1e7},
            "observables": {"delta": delta, "beta": beta,

@@ -427,6 +427,39 @@ cudaError_t measure_logf_bracket(float *max_abs_err, cudaStream_t s)
     return e;
 }
 
+// The same against a table of logarithms (entry k for u = (2k+1) 2^-24).
+__global__ void k_table_bracket(const float *tab, unsigned int *maxbits)
+{
+    unsigned int m = 0;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < (1u << 23); k += gridDim.x * blockDim.x) {
+        const float u = u01f(k << 9);
+        const float e = fabsf(__logf(u) - tab[k]);
+        m = max(m, __float_as_uint(e));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxbits, m);
+}
+
+cudaError_t measure_table_bracket(const float *tab, float *max_abs_err, cudaStream_t s)
+{
+    unsigned int *d = nullptr, h = 0;
+    cudaError_t e = cudaMalloc(&d, sizeof(unsigned int));
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(d, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) {
+        k_table_bracket<<<152 * 8, 256, 0, s>>>(tab, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof h, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d);
+    float f;
+    std::memcpy(&f, &h, sizeof f);
+    *max_abs_err = f;
+    return e;
+}
+
 cudaError_t device_log_eps(int device, cudaStream_t s, double *eps)
 {
     static std::mutex mu;

@@ -15,12 +15,26 @@
 //         host libm's logf (the CPU program) when a table of its values is
 //         given, else CUDA's logf (mcs2).
 // The lattice uses the packed layout of the other sweeps (2-bit codes, rows
-// of 16-site words, [block][word][lane]); FP64 weights and a u32 histogram
-// are staged in shared memory, the lattice too when it fits.
+// of 16-site words, [block][word][lane]); the FP32 difference table of the
+// FP64 weights (stage_diff_table) and a u32 histogram are staged in shared
+// memory, the lattice too when it fits.
+//
+// FP64 issues slowly on this GPU, and the exact log is a table lookup in
+// global memory (host libm values) or a full logf: both used to sit on every
+// attempt's dependency chain.  The test is decided in FP32 instead, as the
+// production scan does it: log(u) < 0 for every u <= 1 - 2^-24, so the
+// reference's test is  log(u) < diff;  with fast = -2 dE + T[E].(dDel)
+// within tol of the FP64 diff and __logf(u) within `log_eps` of the exact
+// log (measured over every u: against CUDA's logf, or against the host
+// table), g = __logf(u) - fast has the sign of log(u) - diff whenever
+// |g| > tol + log_eps.  Otherwise that lane forms the reference's FP64 diff
+// from the global weights and the exact log, so every decision is the
+// reference's.
 #include "sweep_core.cuh"
 
 namespace muca {
 
+// shared memory: the difference table (float2 per bin) | u32 histogram | lattice
 __host__ __device__ inline size_t random_smem_base(uint32_t N)
 {
     return align16((size_t)(N + 1) * 8) + align16((size_t)(N + 1) * 4);
@@ -38,13 +52,12 @@ __global__ void __launch_bounds__(256) k_sweep_random(const RandomArgs a, uint32
         nup = a.dyn[1];
     }
     const uint32_t N = a.N, L = a.L, WPR = a.WPR, nt = blockDim.x, tid = threadIdx.x, lane = threadIdx.x;
-    double *wS = reinterpret_cast<double *>(smem);
+    float2 *T = reinterpret_cast<float2 *>(smem);
     uint32_t *histS = reinterpret_cast<uint32_t *>(smem + align16((size_t)(N + 1) * 8));
     uint32_t *latS = reinterpret_cast<uint32_t *>(smem + random_smem_base(N));
-    for (uint32_t i = tid; i <= N; i += nt) {
-        wS[i] = a.w[i];
-        histS[i] = 0u;
-    }
+    const double *__restrict__ w64 = a.w;
+    const float band = stage_diff_table(w64, N, T) + (float)a.log_eps;
+    for (uint32_t i = tid; i <= N; i += nt) histS[i] = 0u;
     const uint32_t words = L * WPR;
     const bool store = lane < cpb;
     const uint32_t l = store ? lane : 0u;
@@ -97,12 +110,19 @@ __global__ void __launch_bounds__(256) k_sweep_random(const RandomArgs a, uint32
             const int tmp = ns * (os == 0) + os;  // the trial value the reference stores before forming dE
             const int dE = ((os == 0) + os * (ns - os)) * (-tmp) * nb;
             const int dDel = ns * ns - os * os;
-            const double diff = __dsub_rn(__dadd_rn((double)(-dE * 2), wS[E + dDel]), wS[E]);
-            bool acc = diff >= 0.0;
-            if (!acc) {
-                const uint32_t r = pick(r1, sub);
-                const float lg = a.logf_tab ? __ldg(a.logf_tab + (r >> 9)) : logf(u01f(r));
-                acc = (double)lg < diff;
+            const uint32_t r = pick(r1, sub);
+            const float2 tE = T[E];
+            const float dl = dDel == 0 ? 0.0f : (dDel < 0 ? tE.x : tE.y);
+            const float g = __fsub_rn(__logf(u01f(r)), __fadd_rn(small_int_to_float(-2 * dE), dl));
+            bool acc = g < 0.0f;
+            if (fabsf(g) <= band) {
+                // in doubt: the reference's FP64 difference and exact log
+                const double diff = __dsub_rn(__dadd_rn((double)(-dE * 2), w64[E + dDel]), w64[E]);
+                acc = diff >= 0.0;
+                if (!acc) {
+                    const float lg = a.logf_tab ? __ldg(a.logf_tab + (r >> 9)) : logf(u01f(r));
+                    acc = (double)lg < diff;
+                }
             }
             if (acc && store) {
                 const uint32_t sh = 2u * (col & 15u);

@@ -47,6 +47,7 @@ struct muca_ctx {
     unsigned int *d_err = nullptr, *h_err = nullptr;
     uint64_t device_bytes = 0;
     double log_eps = 0, log_eps_measured = 0;
+    double log_eps_table = 1e30;  // host_logf: twice max |__logf(u) - the host table's log(u)|
     uint32_t algo = 0;
     float *d_logf_tab = nullptr;  // random-site algorithm with host_logf: the host libm's logf
     RecScratch rec{};             // the multi-block recursion's dS_i and pair flags (weight mode)
@@ -200,6 +201,8 @@ RandomArgs random_args(muca_ctx *c, uint32_t iter, uint32_t seed, uint64_t therm
     a.nup = nup;
     a.logf_tab = c->d_logf_tab;
     a.dyn = nullptr;
+    // muca_set_log_bracket widens either bound
+    a.log_eps = c->d_logf_tab ? (c->log_eps_table > c->log_eps ? c->log_eps_table : c->log_eps) : c->log_eps;
     return a;
 }
 
@@ -356,6 +359,10 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
             CREATE_TRY(dmalloc(c, &c->d_logf_tab, tab.size()));
             CREATE_TRY(cudaMemcpyAsync(c->d_logf_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, c->stream));
             CREATE_TRY(cudaStreamSynchronize(c->stream));  // `tab` is pageable
+            // the fast test's bound against this table, measured over every entry
+            float m = 0.0f;
+            CREATE_TRY(measure_table_bracket(c->d_logf_tab, &m, c->stream));
+            c->log_eps_table = (m >= 0.0f && m < 1e-2f) ? 2.0 * (double)m + 1e-30 : 1e30;
         }
     }
     CREATE_TRY(cudaStreamSynchronize(c->stream));

@@ -92,7 +92,12 @@ struct RandomArgs {
     unsigned long long therm, nup;
     const float *logf_tab;
     const uint32_t *dyn;  // as SweepArgs::dyn
+    // bound on |__logf(u) - log(u)| over every u01fixedpt<float> value, log
+    // being logf_tab's values (when given) or CUDA's logf, with a safety factor
+    double log_eps;
 };
+// Worst case of |__logf(u) - tab[k]| over u = (2k+1) 2^-24, k < 2^23 (exhaustive, on the device).
+cudaError_t measure_table_bracket(const float *tab, float *max_abs_err, cudaStream_t s);
 size_t random_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem);
 cudaError_t launch_sweep_random(const RandomArgs &a, uint32_t cpb, uint32_t blocks, int rounds, size_t smem_optin,
                                 cudaStream_t s);

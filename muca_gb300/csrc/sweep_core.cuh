@@ -440,6 +440,48 @@ __device__ __noinline__ void partial_core(uint32_t *__restrict__ lat, uint32_t c
     }
 }
 
+// Stages the FP32 differences T[E] = {w[E-1] - w[E], w[E+1] - w[E]} of the
+// FP64 weights w[0..N] in shared memory (every thread of the block calls it)
+// and returns the bound `tol` of the FP32 fast difference
+// fast = f2 + T[E].(dDel) against the reference's FP64
+// diff = ((double)f2 + w[E + dDel]) - w[E], |f2| <= 16:
+//   |fast - diff| <= 2^-24 (|T| + |fast|) + 2^-53 (|w| + 16 + |diff| + |T|),
+// with |T| and |w| reduced over the block, |fast|, |diff| <= 16 + max|T|;
+// twice that.
+__device__ __forceinline__ float stage_diff_table(const double *__restrict__ w64, uint32_t N, float2 *T)
+{
+    __shared__ float s_md[32];
+    __shared__ double s_mw[32];
+    const uint32_t nt = blockDim.x, tid = threadIdx.x;
+    float md = 0.0f;
+    double mw = 0.0;
+    for (uint32_t i = tid; i <= N; i += nt) {
+        const double w0 = w64[i];
+        const float dm = i > 0 ? (float)__dsub_rn(w64[i - 1], w0) : 0.0f;
+        const float dp = i < N ? (float)__dsub_rn(w64[i + 1], w0) : 0.0f;
+        T[i] = make_float2(dm, dp);
+        md = fmaxf(md, fmaxf(fabsf(dm), fabsf(dp)));
+        mw = fmax(mw, fabs(w0));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
+        mw = fmax(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+    }
+    if ((tid & 31u) == 0) { s_md[tid >> 5] = md; s_mw[tid >> 5] = mw; }
+    __syncthreads();
+    if (tid == 0) {
+        for (uint32_t k = 1; k < (nt + 31) / 32; ++k) { md = fmaxf(md, s_md[k]); mw = fmax(mw, s_mw[k]); }
+        const double m = (double)md * 1.0001;
+        s_md[0] = (float)((2.0 * 5.9604644775390625e-8 * (2.0 * m + 16.0) +
+                           2.0 * 1.1102230246251565e-16 * (mw + 32.0 + 2.0 * m)) * 1.0001);
+    }
+    __syncthreads();
+    const float tol = s_md[0];
+    __syncthreads();
+    return tol;
+}
+
 // Stage weights, clear the histogram, stage this block's lattice; returns
 // the lane's lattice base (shared or global).  Only lanes < cpb copy.
 // `blk` is the chain block (blockIdx.x for a single simulation).
@@ -460,37 +502,9 @@ __device__ __forceinline__ uint32_t *prologue(const SweepArgs &a, unsigned char 
     uint32_t *latS = reinterpret_cast<uint32_t *>(smem + lat_offset);
     const WT *wg = reinterpret_cast<const WT *>(a.w);
     if (MODE == kModeProduce && DT) {
-        __shared__ float s_md[32];
-        __shared__ double s_mw[32];
-        float2 *T = reinterpret_cast<float2 *>(smem);
-        const double *w64 = reinterpret_cast<const double *>(a.w);
-        float md = 0.0f;
-        double mw = 0.0;
-        for (uint32_t i = tid; i <= N; i += nt) {
-            const double w0 = w64[i];
-            const float dm = i > 0 ? (float)__dsub_rn(w64[i - 1], w0) : 0.0f;
-            const float dp = i < N ? (float)__dsub_rn(w64[i + 1], w0) : 0.0f;
-            T[i] = make_float2(dm, dp);
-            md = fmaxf(md, fmaxf(fabsf(dm), fabsf(dp)));
-            mw = fmax(mw, fabs(w0));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
-            mw = fmax(mw, __shfl_xor_sync(0xffffffffu, mw, o));
-        }
-        if ((tid & 31u) == 0) { s_md[tid >> 5] = md; s_mw[tid >> 5] = mw; }
-        __syncthreads();
-        if (tid == 0) {
-            for (uint32_t k = 1; k < (nt + 31) / 32; ++k) { md = fmaxf(md, s_md[k]); mw = fmax(mw, s_mw[k]); }
-            // |fast - exact| <= 2^-24 (|T| + |fast|) + 2^-53 (|w| + 16 + |diff| + |T|), |T| <= md,
-            // |fast|, |diff| <= 16 + md; twice that
-            const double m = (double)md * 1.0001;
-            s_md[0] = (float)((2.0 * 5.9604644775390625e-8 * (2.0 * m + 16.0) +
-                               2.0 * 1.1102230246251565e-16 * (mw + 32.0 + 2.0 * m)) * 1.0001);
-        }
-        __syncthreads();
-        if (tol) *tol = s_md[0];
+        const float t = stage_diff_table(reinterpret_cast<const double *>(a.w), N,
+                                         reinterpret_cast<float2 *>(smem));
+        if (tol) *tol = t;
     } else {
         for (uint32_t i = tid; i <= N; i += nt) wS[i] = wg[i];
     }

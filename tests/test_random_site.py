@@ -37,15 +37,28 @@ def _oracle_chains(orc, L, nc, jack, lnw, it, seed, therm, nup, lat, ej, ed):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("host_logf", [1, 0])
-@pytest.mark.parametrize("L,nc,therm,nup", [(16, 4, 0, 5000), (12, 40, 300, 2000), (72, 64, 100, 3000)])
-def test_random_site_sweep_vs_oracle(muca, orc, host_logf, L, nc, therm, nup):
+@pytest.mark.parametrize("L,nc,therm,nup,weights,bracket", [
+    (16, 4, 0, 5000, "walk", None), (12, 40, 300, 2000, "walk", None), (72, 64, 100, 3000, "walk", None),
+    (72, 96, 0, 4000, "muca", None), (16, 40, 100, 3000, "walk", 1e30), (72, 64, 0, 2000, "muca", 1e30)])
+def test_random_site_sweep_vs_oracle(muca, orc, host_logf, L, nc, therm, nup, weights, bracket):
+    """Bit-exact with the oracle; the FP32 fast test decides most attempts and
+    the reference's FP64 test the ones in its band.  bracket = 1e30 sends
+    every attempt to the FP64 test (the exact path on its own).  "muca"
+    weights have the drift of a converged multicanonical weight (range of
+    lnW ~ 3000 at L = 72)."""
     N = L * L
     rng = np.random.default_rng(L + nup)
-    lnw = np.cumsum(rng.normal(0.0, 1.5, N + 1)) * 0.5
+    if weights == "walk":
+        lnw = np.cumsum(rng.normal(0.0, 1.5, N + 1)) * 0.5
+    else:
+        lnw = np.cumsum(rng.normal(-0.6, 0.3, N + 1))
+        lnw -= lnw[0]
     jack, it = 1, 7
     if host_logf:
         orc.use_device_logf(False)  # the CPU program's logf is the host's
     with muca.Engine(L, nchains=nc, algorithm=muca.ALGO_RANDOM_SITE, host_logf=host_logf) as e:
+        if bracket is not None:
+            e.set_log_bracket(bracket)
         e.set_weights(lnw)
         e.init_chains(muca.INIT_MUCA_MAG, jack)
         lat0 = e.get_lattice()
