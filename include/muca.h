@@ -139,7 +139,9 @@ typedef struct muca_run_opts {
     uint32_t nup_schedule;  /* 0: reference ((NUP+1)*1.01 once width==N, :379-382); 1: doubling once
                                width==N; 2: doubling every iteration from the first (cap 2^30);
                                3: as 0, and doubling once every bin also holds >= 5 % of the mean;
-                               4: NUP*1.05 every iteration, the first included (muca_mag.cpp:131) */
+                               4: NUP*1.05 every iteration, the first included (muca_mag.cpp:131);
+                               5: NUP held until width==N, then NUP*1.05 per iteration (the GPU
+                               program's hold, :379-382, with the CPU program's growth, muca_mag.cpp:131) */
     double min_over_mean;   /* threshold for flat_minmean (0 = 0.5) */
     double d_kl_max;        /* threshold of the D_KL test (0 = 1e-4) */
     uint32_t width_start;   /* initial running width (0 = 10, :314); the reference keeps the
@@ -367,7 +369,8 @@ typedef struct muca_batch_run_opts {
     uint32_t nup_schedule;  /* 0: (NUP+1)*1.01 once width == N (:379-382); 1: doubling once width == N;
                                2: doubling every iteration (cap 2^30); 3: as 0, doubling once every
                                bin also holds >= 5 % of the mean count; 4: NUP*1.05 every iteration,
-                               the first included (muca_mag.cpp:131) */
+                               the first included (muca_mag.cpp:131); 5: NUP held until width == N,
+                               then NUP*1.05 per iteration */
     uint32_t flat_minmean;  /* 0: stop at width == N && D_KL < d_kl_max; 1: at min/mean >= min_over_mean */
     uint32_t max_iter;      /* per instance (0 = 1000000) */
     uint32_t graph_iters;   /* iterations per captured graph (0 = 16) */

@@ -32,6 +32,8 @@
 // reference's.
 #include "sweep_core.cuh"
 
+#include <algorithm>
+
 namespace muca {
 
 // shared memory: the difference table (float2 per bin) | u32 histogram | lattice
@@ -161,6 +163,32 @@ static cudaError_t launch_random_one(const RandomArgs &a, uint32_t cpb, uint32_t
     return cudaGetLastError();
 }
 
+// Block shape of the random-site sweep: one wave of blocks over the SMs with
+// the chains spread evenly (ceil(nchains / SMs) per block), each block's
+// lattice in shared memory when that many chains' lattices fit beside the
+// difference table and the histogram.  The random site makes the lattice
+// loads of one attempt depend on the previous attempt's store, so their
+// latency is on every attempt's chain: shared memory, not L1/L2.  When the
+// lattices do not fit, blocks of up to 128 chains read them from global
+// memory.
+SweepPlan plan_random(uint32_t L, uint32_t nchains, size_t smem_optin, int sms)
+{
+    SweepPlan p{};
+    p.mode = kModeWeight;
+    p.kernel = kKernelGeneric;
+    const uint32_t N = L * L, WPR = (L + 15) / 16;
+    const size_t per_chain = (size_t)L * WPR * 4, base = random_smem_base(N);
+    const size_t optin = smem_optin > 512 ? smem_optin - 512 : 0;
+    const size_t cap = optin > base ? (optin - base) / per_chain : 0;
+    const uint32_t want = (nchains + (uint32_t)sms - 1) / (uint32_t)sms;
+    p.lat_smem = cap >= 1 && want <= cap && want <= 256;
+    p.cpb = p.lat_smem ? want : std::min<uint32_t>(128u, want);
+    p.blocks = (nchains + p.cpb - 1) / p.cpb;
+    p.threads = (p.cpb + 31u) / 32u * 32u;
+    p.smem = random_sweep_smem(L, p.cpb, p.lat_smem);
+    return p;
+}
+
 size_t random_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem)
 {
     const uint32_t WPR = (L + 15) / 16;
@@ -171,7 +199,8 @@ cudaError_t launch_sweep_random(const RandomArgs &a, uint32_t cpb, uint32_t bloc
                                 cudaStream_t s)
 {
     if (cpb == 0 || cpb > 256 || a.L < 3) return cudaErrorInvalidValue;
-    const bool ls = random_sweep_smem(a.L, cpb, true) <= smem_optin;
+    // (512 B of the opt-in limit stay free for the kernel's static shared memory)
+    const bool ls = random_sweep_smem(a.L, cpb, true) + 512 <= smem_optin;
     const size_t smem = random_sweep_smem(a.L, cpb, ls);
     if (smem > smem_optin) return cudaErrorInvalidValue;
     if (rounds == 10)

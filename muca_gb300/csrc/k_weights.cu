@@ -151,7 +151,9 @@ __device__ void block_segmented_prefix(int start, int end, double x0, const doub
 // once the width is full and doubling once, in addition, every bin of this
 // iteration's histogram holds at least 5 % of the mean count (`covered`);
 // 4: NUP * 1.05 every iteration, truncated (the CPU program,
-// muca_mag.cpp:131).  The result is capped at `cap` (0: no cap for sched 0,
+// muca_mag.cpp:131); 5: NUP held until the width is full (as the reference
+// GPU program holds it, :379-382), then NUP * 1.05 per iteration (the CPU
+// program's growth).  The result is capped at `cap` (0: no cap for sched 0,
 // 2^30 otherwise) but never falls below nup.
 __host__ __device__ __forceinline__ uint32_t next_nupdates(uint32_t nup, bool full, bool covered, uint32_t sched,
                                                            uint32_t cap)
@@ -163,7 +165,7 @@ __host__ __device__ __forceinline__ uint32_t next_nupdates(uint32_t nup, bool fu
     } else if ((sched == 0 || sched == 3) && full) {
         const unsigned nu = nup + 1u;
         nx = (unsigned)(nu * 1.01);
-    } else if (sched == 4) {
+    } else if (sched == 4 || (sched == 5 && full)) {
         nx = (unsigned long long)((double)nup * 1.05);
         if (cap == 0) cap = 1u << 30;
     }

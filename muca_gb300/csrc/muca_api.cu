@@ -282,7 +282,10 @@ muca_status muca_create(const muca_params *p, muca_ctx **out)
     }
     c->algo = p->algorithm;
     const int want_kernel = p->kernel == 0 ? -1 : (int)p->kernel - 1;
-    c->plan = plan_sweep((int)c->mode, (int)rounds, c->L, c->nchains, c->smem_optin, c->sms, want_kernel);
+    c->plan = c->algo == MUCA_ALGO_RANDOM_SITE
+                  ? plan_random(c->L, c->nchains, c->smem_optin, c->sms)
+                  : plan_sweep((int)c->mode, (int)rounds, c->L, c->nchains, c->smem_optin, c->sms, want_kernel);
+    c->plan.rounds = (int)rounds;
     if (c->plan.smem > c->smem_optin) {
         fail(c, MUCA_ERR_BAD_ARG, "L=%u needs %zu B of shared memory per block (device has %zu)", c->L, c->plan.smem,
              c->smem_optin);
@@ -660,7 +663,7 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
     if (c->mode != MUCA_MODE_WEIGHT) return fail(c, MUCA_ERR_STATE, "weight run needs a weight-mode context");
     if (o->rule > MUCA_UPDATE_RECURSION) return fail(c, MUCA_ERR_BAD_ARG, "rule %u", o->rule);
     if (o->starting_M == 0) return fail(c, MUCA_ERR_BAD_ARG, "starting_M must be >= 1");
-    if (o->nup_schedule > 4) return fail(c, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..4)", o->nup_schedule);
+    if (o->nup_schedule > 5) return fail(c, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..5)", o->nup_schedule);
     CUDA_TRY(c, cudaSetDevice(c->device));
     const auto t0 = std::chrono::steady_clock::now();
     if (o->reinit_chains) {
@@ -689,8 +692,10 @@ static muca_status run_impl(muca_ctx *c, const muca_run_opts *o, muca_run_result
         h.st.nup = nx > cap ? (cap > h.st.nup ? cap : h.st.nup) : (uint32_t)nx;
     } else if (h.st.width == c->N && o->nup_schedule != 2) {
         // (schedule 3 knows no histogram yet: it grows like the reference's)
-        unsigned long long nx = o->nup_schedule == 1 ? 2ull * h.st.nup : (unsigned)((h.st.nup + 1u) * 1.01);
-        const uint32_t cap = o->nup_max ? o->nup_max : (o->nup_schedule == 1 ? (1u << 30) : 0u);
+        unsigned long long nx = o->nup_schedule == 1   ? 2ull * h.st.nup
+                                : o->nup_schedule == 5 ? (unsigned long long)((double)h.st.nup * 1.05)
+                                                       : (unsigned)((h.st.nup + 1u) * 1.01);
+        const uint32_t cap = o->nup_max ? o->nup_max : (o->nup_schedule == 1 || o->nup_schedule == 5 ? (1u << 30) : 0u);
         if (cap != 0 && nx > cap) nx = cap > h.st.nup ? cap : h.st.nup;
         h.st.nup = (uint32_t)nx;
     }

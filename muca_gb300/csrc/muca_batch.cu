@@ -590,7 +590,7 @@ muca_status muca_batch_run(muca_batch *b, const muca_batch_run_opts *o, muca_bat
     if (o->starting_M == 0 && o->starting_sweeps == 0)
         return bfail(b, MUCA_ERR_BAD_ARG, "starting_M or starting_sweeps must be >= 1");
     if (o->starting_sweeps > 4096) return bfail(b, MUCA_ERR_BAD_ARG, "starting_sweeps=%u (at most 4096)", o->starting_sweeps);
-    if (o->nup_schedule > 4) return bfail(b, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..4)", o->nup_schedule);
+    if (o->nup_schedule > 5) return bfail(b, MUCA_ERR_BAD_ARG, "nup_schedule %u (0..5)", o->nup_schedule);
     const uint32_t K = o->graph_iters ? o->graph_iters : 16u;
     if (K > 4096) return bfail(b, MUCA_ERR_BAD_ARG, "graph_iters=%u (at most 4096)", K);
     BCUDA(b, cudaSetDevice(b->device));

@@ -99,6 +99,9 @@ struct RandomArgs {
 // Worst case of |__logf(u) - tab[k]| over u = (2k+1) 2^-24, k < 2^23 (exhaustive, on the device).
 cudaError_t measure_table_bracket(const float *tab, float *max_abs_err, cudaStream_t s);
 size_t random_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem);
+// Block shape of the random-site sweep for (L, nchains) on a device with
+// `smem_optin` bytes of opt-in shared memory per block and `sms` SMs.
+SweepPlan plan_random(uint32_t L, uint32_t nchains, size_t smem_optin, int sms);
 cudaError_t launch_sweep_random(const RandomArgs &a, uint32_t cpb, uint32_t blocks, int rounds, size_t smem_optin,
                                 cudaStream_t s);
 

@@ -27,8 +27,10 @@ import numpy as np
 import muca_gb300 as m
 
 # the weight iteration used for the training data and both arms of the A/B
-RUN_OPTS = dict(starting_M=1, rule=m.UPDATE_TRIVIAL, nup_schedule=1, flat_minmean=1, max_iter=8000,
-                graph_iters=32, starting_sweeps=1, nup_max=1 << 18)
+# (schedule 5: NUPDATES held until the width is N, then x1.05 per iteration;
+# one schedule for every arm)
+RUN_OPTS = dict(starting_M=1, rule=m.UPDATE_TRIVIAL, nup_schedule=5, flat_minmean=1, max_iter=20000,
+                graph_iters=32, starting_sweeps=1, nup_max=1 << 20)
 
 
 def converge(instances, opts=RUN_OPTS, warm=None, device=0):
@@ -182,65 +184,126 @@ def ab_test(net, held, opts=RUN_OPTS, device=0, sources=None, graded=False):
     return out
 
 
+def final_agreement(arm_w, zero_w):
+    """The converged weights of an arm against the zero arm's, both shifted
+    to mean zero: rms and max |difference| in lnW, and the rms relative to
+    the range of lnW."""
+    f = np.asarray(arm_w) - np.asarray(zero_w)
+    f = f - f.mean()
+    rng_ = float(np.max(zero_w) - np.min(zero_w))
+    rms = float(np.sqrt(np.mean(f * f)))
+    return {"rms": rms, "max": float(np.max(np.abs(f))), "rms_rel_range": rms / rng_ if rng_ > 0 else None}
+
+
+def agreement_under(net, held, sources, opts, device=0):
+    """The arms run to `opts`' stop criterion; each arm's converged weights
+    against the zero arm's, beside the statistical floor (the zero weight on
+    other seeds against the zero weight)."""
+    arms = {"mlp": [net.log_weights(L, T, D) for L, _, T, D, _ in held],
+            "interp": [interpolated_weight(L, T, sources) for L, _, T, _, _ in held],
+            "pl": [interpolated_weight(L, T, sources, PL_KNOTS) for L, _, T, _, _ in held]}
+    rz, sz, wz = converge(held, opts, None, device)
+    out = {"zero": {"iters_total": sum(r.iterations for r in rz), "device_s": sz,
+                    "converged": sum(bool(r.converged) for r in rz)}}
+    floor_runs = converge([(L, nc, T, D, seed + 7919) for L, nc, T, D, seed in held], opts, None, device)
+    runs = dict(arms)
+    per = {k: [] for k in list(arms) + ["zero_reseeded"]}
+    for k, w0 in runs.items():
+        r, sec, wf = converge(held, opts, w0, device)
+        out[k] = {"iters_total": sum(x.iterations for x in r), "device_s": sec,
+                  "converged": sum(bool(x.converged) for x in r)}
+        per[k] = [final_agreement(wf[i], wz[i]) for i in range(len(held))]
+    rf, sf, wff = floor_runs
+    out["zero_reseeded"] = {"iters_total": sum(x.iterations for x in rf), "device_s": sf,
+                            "converged": sum(bool(x.converged) for x in rf)}
+    per["zero_reseeded"] = [final_agreement(wff[i], wz[i]) for i in range(len(held))]
+    for k, v in per.items():
+        out[k]["final_rms_vs_zero_median"] = float(np.median([a["rms"] for a in v]))
+        out[k]["final_rms_vs_zero_max"] = float(np.max([a["rms"] for a in v]))
+        out[k]["final_rms_rel_range_max"] = float(np.max([a["rms_rel_range"] for a in v]))
+        out[k]["final_maxabs_vs_zero_max"] = float(np.max([a["max"] for a in v]))
+        out[k]["per_instance_rms"] = [round(a["rms"], 5) for a in v]
+    return out
+
+
+def held_out_instances(Ls, Ts, rng, chains):
+    return [(L, chains, float(T), float(rng.uniform(1.5, 1.99)), 5000 + k)
+            for k, (L, T) in enumerate([(L, float(T)) for L in Ls for T in Ts])]
+
+
+def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, held_T=(0.43, 0.53, 0.63, 0.73),
+              held_L=(), schedule=5, steps=10000, device=0, reference_criterion=True, graded=False,
+              ab_schedules=()):
+    """The whole study: training data from the batched engine (every (L, T)
+    on the grid, seed per instance), the network trained on the device, the
+    A/B on the held-out (L, T, Delta) to min/mean >= 0.5 with one NUPDATES
+    schedule for every arm, and (reference_criterion) the same arms run to
+    the reference's criterion (width == N and D_KL < 1e-4) for the
+    agreement of the final weights."""
+    t_all = time.time()
+    Ts = np.round(np.arange(0.40, 0.8 + 1e-9, t_step), 4)
+    rng = np.random.default_rng(0)
+    opts = dict(RUN_OPTS, nup_schedule=schedule)
+    train_inst = [(L, chains, float(T), float(rng.uniform(1.5, 1.99)), 1000 + k)
+                  for k, (L, T) in enumerate([(L, T) for L in Ls for T in Ts])]
+    t0 = time.time()
+    res, sec, W = converge(train_inst, opts, None, device)
+    ok = [i for i, r in enumerate(res) if r.converged]
+    x, t = training_set([train_inst[i] for i in ok], [W[i] for i in ok])
+    gen = {"instances": len(train_inst), "sizes": list(Ls), "chains": chains, "converged": len(ok),
+           "device_s": sec, "wall_s": time.time() - t0,
+           "iters_median": float(np.median([r.iterations for r in res])),
+           "iters_max": int(max(r.iterations for r in res)), "points": int(x.shape[0])}
+    out = {"run_opts": dict(opts), "training_set": gen}
+    with m.MLP(device=device, seed=7) as net:
+        t0 = time.time()
+        sched = ((steps, 1e-3), (steps, 3e-4), (steps, 1e-4))
+        losses = train(net, x, t, schedule=sched)
+        fit_s = time.time() - t0
+        flops = 3 * losses.size * 4096 * 2 * net.n_params  # forward + backward: ~3 x 2 flop per weight and point
+        out["fit"] = {"steps": int(losses.size), "batch": 4096, "lr": [s_[1] for s_ in sched],
+                      "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
+                      "wall_s": fit_s, "tflops": flops / fit_s / 1e12}
+        held = held_out_instances(list(Ls) + list(held_L), held_T, rng, chains)
+        sources = [(train_inst[i][0], train_inst[i][2], W[i]) for i in ok]
+        t0 = time.time()
+        ab = ab_test(net, held, opts, device, sources, graded=graded)
+        ab["wall_s"] = time.time() - t0
+        out["ab"] = ab
+        if reference_criterion:
+            ro = dict(opts, flat_minmean=0, max_iter=40000)
+            t0 = time.time()
+            out["agreement_reference_criterion"] = agreement_under(net, held, sources, ro, device)
+            out["agreement_reference_criterion"]["wall_s"] = time.time() - t0
+        ab_sched = {int(sc): ab_test(net, held, dict(opts, nup_schedule=int(sc)), device, sources)
+                    for sc in ab_schedules}
+        if ab_sched:
+            out["ab_schedules"] = ab_sched
+    out["wall_s"] = time.time() - t_all
+    return out
+
+
 def main(argv=None):
     p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    p.add_argument("--L", default="16,24,32,48")
-    p.add_argument("--chains", type=int, default=1024)
+    p.add_argument("--L", default="16,24,32,48,64,72,96,128")
+    p.add_argument("--chains", type=int, default=256)
     p.add_argument("--t-step", type=float, default=0.025)
-    p.add_argument("--held-T", default="0.53,0.67")
+    p.add_argument("--held-T", default="0.43,0.53,0.63,0.73")
     p.add_argument("--held-L", default="", help="held-out lattice sizes beyond the training ones")
     p.add_argument("--graded", action="store_true", help="also run the arms from graded initial spins")
     p.add_argument("--steps", type=int, default=10000, help="Adam steps per learning-rate stage (3 stages)")
-    p.add_argument("--schedule", type=int, default=RUN_OPTS["nup_schedule"])
+    p.add_argument("--schedule", type=int, default=5, help="NUPDATES schedule of every arm")
     p.add_argument("--ab-schedules", default="",
                    help="NUPDATES schedules to repeat the A/B with (same network), e.g. 0,4")
+    p.add_argument("--no-reference-criterion", action="store_true",
+                   help="skip the runs to width == N and D_KL < 1e-4")
     p.add_argument("--device", type=int, default=0)
     a = p.parse_args(argv)
-    Ls = [int(v) for v in a.L.split(",")]
-    held_L = [int(v) for v in a.held_L.split(",") if v]
-    Ts = np.round(np.arange(0.40, 0.8 + 1e-9, a.t_step), 4)
-    rng = np.random.default_rng(0)
-    opts = dict(RUN_OPTS, nup_schedule=a.schedule)
-    train_inst = [(L, a.chains, float(T), float(rng.uniform(1.5, 1.99)), 1000 + k)
-                  for k, (L, T) in enumerate([(L, T) for L in Ls for T in Ts])]
-    t0 = time.time()
-    res, sec, W = converge(train_inst, opts, None, a.device)
-    ok = [i for i, r in enumerate(res) if r.converged]
-    x, t = training_set([train_inst[i] for i in ok], [W[i] for i in ok])
-    gen = {"instances": len(train_inst), "converged": len(ok), "device_s": sec, "wall_s": time.time() - t0,
-           "iters_median": float(np.median([r.iterations for r in res])), "points": int(x.shape[0])}
-    with m.MLP(device=a.device, seed=7) as net:
-        t0 = time.time()
-        sched = ((a.steps, 1e-3), (a.steps, 3e-4), (a.steps, 1e-4))
-        losses = train(net, x, t, schedule=sched)
-        fit = {"steps": int(losses.size), "batch": 4096, "lr": [s[1] for s in sched],
-               "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
-               "wall_s": time.time() - t0}
-        held = [(L, a.chains, float(T), float(rng.uniform(1.5, 1.99)), 5000 + k)
-                for k, (L, T) in enumerate([(L, float(T)) for L in Ls + held_L for T in a.held_T.split(",")])]
-        sources = [(train_inst[i][0], train_inst[i][2], W[i]) for i in ok]
-        ab = ab_test(net, held, opts, a.device, sources, graded=a.graded)
-        # the A/B under other NUPDATES schedules, both arms alike (the network is the same)
-        ab_sched = {int(sc): ab_test(net, held, dict(opts, nup_schedule=int(sc)), a.device, sources)
-                    for sc in a.ab_schedules.split(",") if sc}
-        if ab_sched:
-            # each start with its own best schedule against the reference's method
-            # (zero weight, schedule 0), from the runs above
-            best = {}
-            for arm in ("zero", "mlp", "pl", "interp"):
-                cand = [(v[arm + "_device_s"], sc, v[arm + "_iters_total"])
-                        for sc, v in list(ab_sched.items()) + [(opts["nup_schedule"], ab)]]
-                t, sc, it = min(cand)
-                best[arm] = {"schedule": sc, "device_s": t, "iters_total": it}
-            if 0 in ab_sched:
-                ref = ab_sched[0]
-                for arm in best:
-                    best[arm]["iters_ratio_vs_reference_method"] = ref["zero_iters_total"] / best[arm]["iters_total"]
-                    best[arm]["time_ratio_vs_reference_method"] = ref["zero_device_s"] / best[arm]["device_s"]
-            ab_sched["best_schedule_per_arm"] = best
-    out = {"run_opts": {k: v for k, v in opts.items()}, "training_set": gen, "fit": fit, "ab": ab}
-    if ab_sched:
-        out["ab_schedules"] = ab_sched
+    out = run_study(Ls=[int(v) for v in a.L.split(",")], chains=a.chains, t_step=a.t_step,
+                    held_T=[float(v) for v in a.held_T.split(",")],
+                    held_L=[int(v) for v in a.held_L.split(",") if v], schedule=a.schedule, steps=a.steps,
+                    device=a.device, reference_criterion=not a.no_reference_criterion, graded=a.graded,
+                    ab_schedules=[int(v) for v in a.ab_schedules.split(",") if v])
     print(json.dumps(out))
     return out
 

@@ -631,7 +631,7 @@ unsigned orc_weight_run(const orc_weight_opts *o, int8_t *lat, int32_t *ej, int3
             } else if ((o->sched == 0 || o->sched == 3) && width == N) {
                 const unsigned nu = NUPDATES + 1;
                 nx = (unsigned)(nu * 1.01);
-            } else if (o->sched == 4) {
+            } else if (o->sched == 4 || (o->sched == 5 && width == N)) {
                 nx = (uint64_t)((double)NUPDATES * 1.05);
                 if (cap == 0) cap = 1u << 30;
             }

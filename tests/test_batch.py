@@ -93,7 +93,7 @@ def test_batch_graded_init_equals_single_simulations(muca):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("sched", [0, 3, 4])
+@pytest.mark.parametrize("sched", [0, 3, 4, 5])
 def test_batch_schedules_equal_single_simulations(muca, sched):
     kw = dict(nup_schedule=sched, flat_minmean=1, max_iter=25, nup_max=1 << 14)
     inst = INSTANCES[:3]

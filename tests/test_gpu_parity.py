@@ -363,7 +363,7 @@ def test_weight_update_vs_oracle(muca, orc, rule, N):
 
 @pytest.mark.parametrize("rule,hold,flat,sched", [(0, 0, 0, 0), (2, 0, 0, 0), (0, 1, 0, 0), (0, 0, 1, 0),
                                                    (1, 0, 0, 0), (0, 0, 1, 1), (2, 0, 1, 2), (0, 0, 1, 2),
-                                                   (0, 0, 1, 3)])
+                                                   (0, 0, 1, 3), (0, 0, 1, 5), (0, 0, 0, 5)])
 def test_weight_run_vs_oracle(muca, orc, rule, hold, flat, sched):
     """Whole reference iteration loop (schedule, width, D_KL, update) on the
     device against orc_weight_run, iteration by iteration; sched 1, 2 and 3
@@ -371,8 +371,8 @@ def test_weight_run_vs_oracle(muca, orc, rule, hold, flat, sched):
     every bin is covered)."""
     # doubling every iteration: few iterations, so the oracle stays quick
     L, cpd, max_iter = 8, 256, (14 if sched == 2 else 60)
-    nup_max = 3000 if sched in (1, 3) else 0
-    M = 64 if sched in (1, 3) else 1  # reaches full width, then doubles up to the cap
+    nup_max = 3000 if sched in (1, 3, 5) else 0
+    M = 64 if sched in (1, 3, 5) else 1  # reaches full width, then grows up to the cap
     N = L * L
     with muca.Engine(L, nchains=cpd) as e:
         res, recs = e.weight_run(starting_M=M, jack=0, rule=rule, hold_until_full=hold, flat_minmean=flat,

@@ -121,5 +121,6 @@ def test_observables_agree_with_the_cpu_program_within_jackknife_errors(orc, con
         ca, ce = orc.jackknife(per_block[:, i])
         ga, ge = jk[i]
         z = abs(ga - ca) / np.hypot(ge, ce)
+        print("%s: device %.8g +- %.2g, CPU program %.8g +- %.2g: %.2f sigma" % (names[i], ga, ge, ca, ce, z))
         assert np.isfinite(z) and z < 3.0, "%s: device %.6g +- %.2g, CPU program %.6g +- %.2g (%.2f sigma)" % (
             names[i], ga, ge, ca, ce, z)
