@@ -69,7 +69,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ref-gpu", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the flat-run, batch and production lines")
-    p.add_argument("--only", choices=["flat_run", "config2", "batch", "production", "random_site"],
+    p.add_argument("--only", choices=["flat_run", "config2", "batch", "production", "random_site", "warm_start"],
                    help="run only this extra line and print it (for profiling a smaller case)")
     p.add_argument("--production-L", type=int, default=128, help="lattice size of --only production")
     p.add_argument("--blocks", type=int, default=10, help="jackknife blocks of --only production")
@@ -512,6 +512,28 @@ def config2_metric(local, steps=10):
     return out
 
 
+def warm_start_metric(local):
+    """The learned warm start (the L=72 configuration's second metric with the
+    network's initial weight, on the batched configuration's instances):
+    converged weights of every (L, T) on a grid (L in {16..128}, 256 chains
+    each) train the MLP on the device; 32 held-out (L, T, Delta) then run the
+    weight iteration from the zero weight, from the network's weight and from
+    two non-learned starts, one NUPDATES schedule for every arm, to
+    min/mean >= 0.5 (iterations, device and wall time) and to the
+    reference's criterion width == N and D_KL < 1e-4 (agreement of the final
+    weights with the zero arm's, beside the zero weight on other seeds).
+    Minutes of GPU time: not part of the default line."""
+    from muca_gb300 import warm_start as ws
+    out = ws.run_study(device=local)
+    ab = out["ab"]
+    out["summary"] = {
+        "iters_ratio_mlp_vs_zero": ab["mlp_iters_ratio"], "device_time_ratio_mlp_vs_zero": ab["mlp_time_ratio"],
+        "iters_ratio_interp_vs_zero": ab["interp_iters_ratio"],
+        "device_time_ratio_interp_vs_zero": ab["interp_time_ratio"],
+        "iters_ratio_pl_vs_zero": ab["pl_iters_ratio"], "device_time_ratio_pl_vs_zero": ab["pl_time_ratio"]}
+    return out
+
+
 def batch_metric(local, iters=32):
     """The batched engine on 256 uneven instances (L in {16..128}, T in
     [0.4, 0.8], 256 chains each, seed = instance id): device throughput of
@@ -792,7 +814,7 @@ def main():
         from muca_gb300 import build as b
         b.build()
         fn = {"flat_run": flat_run_metric, "config2": config2_metric, "batch": batch_metric,
-              "random_site": random_site_metric,
+              "random_site": random_site_metric, "warm_start": warm_start_metric,
               "production": lambda d: production_metric(d, args.production_L, with_ref=False, kernel=args.kernel,
                                                         blocks=args.blocks, block_sweeps=args.block_sweeps,
                                                         therm_sweeps=args.therm_sweeps,

@@ -275,7 +275,11 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
             t0 = time.time()
             out["agreement_reference_criterion"] = agreement_under(net, held, sources, ro, device)
             out["agreement_reference_criterion"]["wall_s"] = time.time() - t0
-        ab_sched = {int(sc): ab_test(net, held, dict(opts, nup_schedule=int(sc)), device, sources)
+        # the A/B under other NUPDATES schedules (the same network; every arm
+        # alike); NUPDATES capped at 2^16 there, which keeps schedule 4's
+        # zero arm (x1.05 from the first iteration, through thousands of
+        # width-growing iterations at L = 128) within minutes
+        ab_sched = {int(sc): ab_test(net, held, dict(opts, nup_schedule=int(sc), nup_max=1 << 16), device, sources)
                     for sc in ab_schedules}
         if ab_sched:
             out["ab_schedules"] = ab_sched
