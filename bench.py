@@ -69,12 +69,15 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ref-gpu", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the flat-run, batch and production lines")
-    p.add_argument("--only", choices=["flat_run", "config2", "batch", "production", "random_site", "warm_start"],
+    p.add_argument("--only", choices=["flat_run", "config2", "batch", "production", "random_site", "warm_start",
+                                      "mlp"],
                    help="run only this extra line and print it (for profiling a smaller case)")
     p.add_argument("--production-L", type=int, default=128, help="lattice size of --only production")
     p.add_argument("--blocks", type=int, default=10, help="jackknife blocks of --only production")
     p.add_argument("--block-sweeps", type=int, default=100, help="production sweeps per block of --only production")
     p.add_argument("--therm-sweeps", type=int, default=100, help="thermalisation sweeps of --only production")
+    p.add_argument("--state-out", default=None, help="--only production: save the converged weight and lattices")
+    p.add_argument("--state-in", default=None, help="--only production: start from a saved state (no weight run)")
     p.add_argument("--kernel", type=int, default=0, help="sweep kernel: 0 auto, 1 generic, 2 windowed, 3 specialised")
     return p.parse_args()
 
@@ -534,6 +537,34 @@ def warm_start_metric(local):
     return out
 
 
+def mlp_metric(local, steps=2048, batch=4096):
+    """Training throughput of the warm-start network on this GPU: `steps`
+    Adam steps (minibatch gather, forward, backward, weight gradients,
+    update; 32 steps per CUDA graph) at batch 4096 on a synthetic set of the
+    warm start's size (663,816 points: every bin of 17 temperatures at each
+    L in {16..128}).  FLOPs per step: 6 x parameters x batch (the forward
+    product, and the two backward products)."""
+    import numpy as np
+    import muca_gb300 as m
+    rng = np.random.default_rng(0)
+    n = 663816
+    x = np.stack([rng.choice([16, 24, 32, 48, 64, 72, 96, 128], n) / 128.0, rng.uniform(0.4, 0.8, n),
+                  rng.uniform(1.5, 1.99, n), rng.uniform(0.0, 1.0, n)], axis=1).astype(np.float32)
+    t = (np.sin(3.0 * x[:, 3]) * x[:, 1] - 0.5 * x[:, 0] * x[:, 3] ** 2).astype(np.float32)
+    with m.MLP(device=local, seed=1) as net:
+        net.set_data(x, t)
+        net.train(64, batch=batch, lr=1e-3, seed=2)  # warm-up: graph capture, scratch
+        t0 = time.perf_counter()
+        losses = net.train(steps, batch=batch, lr=1e-3, seed=3)
+        dt = time.perf_counter() - t0
+        flops = 6.0 * net.n_params * batch * steps
+    return {"metric": "warm-start network training throughput", "steps": steps, "batch": batch,
+            "params": int(net.n_params), "s": dt, "steps_per_s": steps / dt, "tflops": flops / dt / 1e12,
+            "unit": "TFLOP/s (FP32, CUDA cores)", "loss_first": float(losses[:8].mean()),
+            "loss_last": float(losses[-64:].mean()),
+            "timing": "host clock around the train call (graph replays and one synchronisation)"}
+
+
 def batch_metric(local, iters=32):
     """The batched engine on 256 uneven instances (L in {16..128}, T in
     [0.4, 0.8], 256 chains each, seed = instance id): device throughput of
@@ -677,7 +708,7 @@ def cpu_produce_rate(L, lnw, nthreads, min_seconds=10.0):
 
 
 def production_metric(local, L=128, with_ref=True, kernel=0, blocks=10, therm_sweeps=100, block_sweeps=100,
-                      with_cpu=True):
+                      with_cpu=True, state_in=None, state_out=None):
     """The L=128 production configuration with its shapes and scaled sweep
     counts: a converged L=128 weight (converge_weight), 16384 chains from the
     reference production initialisation, `therm_sweeps` thermalisation
@@ -694,7 +725,11 @@ def production_metric(local, L=128, with_ref=True, kernel=0, blocks=10, therm_sw
     instead of fresh random spins (E_Delta ~ 2N/3 for every chain): from
     there no block would sample the E_Delta that dominate the reweighting at
     Delta = 1.96, and every Boltzmann factor of the rows it did sample would
-    underflow."""
+    underflow.
+
+    state_out / state_in: save the converged weight and lattices to an .npz
+    file, or start from one instead of converging (to profile the
+    production sweep alone)."""
     import numpy as np
     import torch
     import muca_gb300 as m
@@ -702,7 +737,13 @@ def production_metric(local, L=128, with_ref=True, kernel=0, blocks=10, therm_sw
     N = L * L
     beta, delta = 2.0, 1.96
     stream = torch.cuda.Stream()
-    w, lat_w, wsum = converge_weight(L, local, nc, stream.cuda_stream)
+    if state_in:
+        st = np.load(state_in)
+        w, lat_w, wsum = st["w"], st["lat"], {"from": "saved state", "L": L}
+    else:
+        w, lat_w, wsum = converge_weight(L, local, nc, stream.cuda_stream)
+    if state_out:
+        np.savez(state_out, w=w, lat=lat_w)
     per_block = []
     with m.Engine(L, nchains=nc, device=local, mode=m.MODE_PRODUCE, stream=stream.cuda_stream, kernel=kernel) as e:
         e.set_lattice(lat_w)  # the equilibrated multicanonical walkers
@@ -814,11 +855,12 @@ def main():
         from muca_gb300 import build as b
         b.build()
         fn = {"flat_run": flat_run_metric, "config2": config2_metric, "batch": batch_metric,
-              "random_site": random_site_metric, "warm_start": warm_start_metric,
+              "random_site": random_site_metric, "warm_start": warm_start_metric, "mlp": mlp_metric,
               "production": lambda d: production_metric(d, args.production_L, with_ref=False, kernel=args.kernel,
                                                         blocks=args.blocks, block_sweeps=args.block_sweeps,
                                                         therm_sweeps=args.therm_sweeps,
-                                                        with_cpu=not args.no_cpu_baseline)}[args.only]
+                                                        with_cpu=not args.no_cpu_baseline,
+                                                        state_in=args.state_in, state_out=args.state_out)}[args.only]
         print(json.dumps(fn(local)))
         return 0
     return ours_arm(args, ws, rank, local)

@@ -55,18 +55,20 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep(const BatchInst *__restr
         if (launch_params(a, iter, nup)) {  // the instance is still running
             if (threadIdx.x < 17) s_btab[threadIdx.x] = I->btab[threadIdx.x];
             // s_btab is read only after the block barrier inside the sweep's prologue
-            if (LAT == kLatWhereFits) {
+            if (LAT == kLatShared) {
+                win_sweep_block<kModeWeight, R, true, HS, true>(a, smem, cpb, item.blk, iter, nup, s_btab);
+            } else {
                 // uniform per item: the lattice joins the weights (and bins) in
                 // shared memory when all fit in the launch's allocation
-                const size_t need = smem_weights_bytes(kModeWeight, a.N) +
-                                    (HS ? smem_hist_bytes(kModeWeight, a.N) : 0) + (size_t)a.L * a.WPR * 4u * cpb;
-                if (need <= smem_bytes)
+                // (kLatWhereFits); otherwise it stays in global memory, behind
+                // a four-row ring per lane where that fits
+                const size_t base = smem_weights_bytes(kModeWeight, a.N) + (HS ? smem_hist_bytes(kModeWeight, a.N) : 0);
+                if (LAT == kLatWhereFits && base + (size_t)a.L * a.WPR * 4u * cpb <= smem_bytes)
                     win_sweep_block<kModeWeight, R, true, HS, true>(a, smem, cpb, item.blk, iter, nup, s_btab);
+                else if (a.L % 4 == 0 && a.WPR <= 8 && base + ring_bytes(a.L, cpb) <= smem_bytes)
+                    win_sweep_block<kModeWeight, R, false, HS, true, true>(a, smem, cpb, item.blk, iter, nup, s_btab);
                 else
                     win_sweep_block<kModeWeight, R, false, HS, true>(a, smem, cpb, item.blk, iter, nup, s_btab);
-            } else {
-                win_sweep_block<kModeWeight, R, LAT == kLatShared, HS, true>(a, smem, cpb, item.blk, iter, nup,
-                                                                            s_btab);
             }
         }
         __syncthreads();
@@ -80,11 +82,11 @@ cudaError_t launch_batch_prep(const BatchInst *insts, uint32_t n_inst, uint32_t 
     return cudaGetLastError();
 }
 
-size_t batch_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem, bool hist_smem)
+size_t batch_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem, bool hist_smem, bool row_ring)
 {
     const uint32_t N = L * L, WPR = (L + 15) / 16;
     return smem_weights_bytes(kModeWeight, N) + (hist_smem ? smem_hist_bytes(kModeWeight, N) : 0) +
-           (lat_smem ? (size_t)L * WPR * 4 * cpb : 0);
+           (lat_smem ? (size_t)L * WPR * 4 * cpb : (row_ring ? ring_bytes(L, cpb) : 0));
 }
 
 using BatchKernel = void (*)(const BatchInst *, const BatchItem *, uint32_t, uint32_t *, uint32_t, uint32_t);

@@ -46,14 +46,15 @@ namespace muca {
 
 // ---------------------------------------------------------------------------
 // Windowed kernel: one block per chain block, blockDim = cpb rounded up to a warp.
-template <int MODE, int R, bool LAT_SMEM>
+// RING: the lattice stays in global memory behind a four-row ring per lane.
+template <int MODE, int R, bool LAT_SMEM, bool RING = false>
 __global__ void __launch_bounds__(256, 1) k_sweep_win(const SweepArgs a, uint32_t cpb)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t iter;
     unsigned long long nup;
     if (!launch_params(a, iter, nup)) return;
-    win_sweep_block<MODE, R, LAT_SMEM>(a, smem, cpb, blockIdx.x, iter, nup);
+    win_sweep_block<MODE, R, LAT_SMEM, true, false, RING>(a, smem, cpb, blockIdx.x, iter, nup);
 }
 
 // ---------------------------------------------------------------------------
@@ -524,17 +525,22 @@ SweepPlan plan_sweep(int mode, int rounds, uint32_t L, uint32_t nchains, size_t 
     p.blocks = (nchains + cpb - 1) / cpb;
     const uint32_t warps = (cpb + 31u) / 32u;
     p.threads = (p.kernel == kKernelSpecialized ? 2u : 1u) * warps * 32u;
+    // a lattice in global memory: the windowed kernel keeps a four-row ring
+    // per lane in shared memory when it fits
+    p.row_ring = !p.lat_smem && p.kernel == kKernelWindowed && L % 4 == 0 && WPR <= 8 &&
+                 base + ring_bytes(L, cpb) <= optin;
     p.smem = base + (p.kernel == kKernelSpecialized ? smem_ring_bytes(warps) : 0) +
-             (p.lat_smem ? per_chain * cpb : 0);
+             (p.lat_smem ? per_chain * cpb : 0) + (p.row_ring ? ring_bytes(L, cpb) : 0);
     return p;
 }
 
 template <int MODE, int R, bool LS>
 static cudaError_t launch_one(const SweepPlan &p, const SweepArgs &a, cudaStream_t s)
 {
-    void (*kern)(const SweepArgs, uint32_t) = p.kernel == kKernelSpecialized ? k_sweep_spec<MODE, R, LS>
-                                            : p.kernel == kKernelWindowed    ? k_sweep_win<MODE, R, LS>
-                                                                             : k_sweep_generic<MODE, R, LS>;
+    void (*kern)(const SweepArgs, uint32_t) =
+        p.kernel == kKernelSpecialized ? k_sweep_spec<MODE, R, LS>
+        : p.kernel == kKernelWindowed  ? (!LS && p.row_ring ? k_sweep_win<MODE, R, false, true> : k_sweep_win<MODE, R, LS>)
+                                       : k_sweep_generic<MODE, R, LS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
     if (e != cudaSuccess) return e;
     kern<<<p.blocks, p.threads, p.smem, s>>>(a, p.cpb);

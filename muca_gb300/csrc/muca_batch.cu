@@ -211,13 +211,16 @@ size_t smem_budget(const muca_batch *b) { return b->smem_optin > 1024 ? b->smem_
 // Launch shared memory of a shape: the largest block over the instances, each
 // with its lattice in shared memory where the shape puts it there
 // (kLatWhereFits: where the block stays within the budget; the sweep kernel
-// makes the same choice per instance against the launch's size).
+// makes the same choice per instance against the launch's size), and a
+// lattice left in global memory with its four-row ring where that fits the
+// budget (the kernel again decides per instance against the launch's size).
 size_t shape_smem(const muca_batch *b, uint32_t cpb, uint32_t lat, bool hist_smem)
 {
     size_t smem = 0;
     for (const muca_instance &m : b->inst) {
         const size_t with = batch_sweep_smem(m.L, cpb, true, hist_smem);
-        const size_t without = batch_sweep_smem(m.L, cpb, false, hist_smem);
+        const size_t ring = batch_sweep_smem(m.L, cpb, false, hist_smem, true);
+        const size_t without = ring <= smem_budget(b) ? ring : batch_sweep_smem(m.L, cpb, false, hist_smem);
         const bool in = lat == kLatShared || (lat == kLatWhereFits && with <= smem_budget(b));
         smem = std::max(smem, in ? with : without);
     }

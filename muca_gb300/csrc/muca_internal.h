@@ -57,6 +57,7 @@ struct SweepPlan {
     int kernel;      // SweepKernel
     bool fast;       // windowed kernels usable (L % 8 == 0)
     bool lat_smem;   // lattice resident in shared memory
+    bool row_ring;   // lattice in global memory behind a four-row ring per lane (windowed kernel)
     uint32_t cpb;    // chains per block (lane stride of the packed lattice)
     uint32_t threads;  // threads per block
     uint32_t blocks;
@@ -218,8 +219,8 @@ cudaError_t launch_batch_sweep(const BatchInst *insts, const BatchItem *items, u
                                uint32_t cpb, int rounds, uint32_t lat, bool hist_smem, uint32_t grid, size_t smem,
                                cudaStream_t s);
 // Dynamic shared memory of one batch sweep block for an instance of size L,
-// with or without its lattice.
-size_t batch_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem, bool hist_smem);
+// with its lattice, or without it (then optionally with its four-row ring).
+size_t batch_sweep_smem(uint32_t L, uint32_t cpb, bool lat_smem, bool hist_smem, bool row_ring = false);
 // Blocks of the batch sweep that fit on one SM with `smem` bytes each; also
 // sets the kernel's shared-memory limit to `smem` (call before any capture).
 // The launch with that shape needs no further attribute call.
@@ -258,7 +259,8 @@ cudaError_t launch_observables_static(int device, const unsigned long long *hist
 // Warm-start MLP (k_mlp.cu): 4 -> 128 -> 128 -> 128 -> 1, SiLU, FP32.
 size_t mlp_param_count();
 cudaError_t mlp_prepare();  // shared-memory limits (call before any capture)
-// scratch floats of a minibatch of B points: Xb [B][4], Tb [B], Y [B], Z, dZ, partials
+// scratch floats of a minibatch of B points: Xb [B][4] at 0, Tb [B] at 4B,
+// Y [B] at 5B, then (aligned) Z, dZ and partials
 size_t mlp_scratch_floats(uint32_t B);
 // Y[0..B) = net(Xb) (Z: pre-activations [3][B][128] or NULL)
 cudaError_t launch_mlp_forward(const float *P, const float *Xb, uint32_t B, float *Z, float *Y, cudaStream_t s);

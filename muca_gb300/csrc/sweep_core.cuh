@@ -151,24 +151,29 @@ struct WinDec {
 // BT: -beta*dE comes from the table btab[dE + 8] (any beta) instead of the
 // reference's literal -2 dE (beta = 2); the table holds (float)(-beta*dE),
 // which for beta = 2 is the same value.
+// rmask: rows are addressed as (row & rmask): ~0u for a whole lattice,
+// 3 for the four-row ring of RowRing (L is a multiple of 4, so the ring's
+// slots follow the periodic rows).
 template <int MODE, int SLOTS, bool BT = false>
 __device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
                                               uint32_t row, uint32_t q, uint32_t half, const uint32_t *r1,
-                                              const uint32_t *r3, const float *__restrict__ btab, WinDec<MODE> &d)
+                                              const uint32_t *r3, const float *__restrict__ btab, WinDec<MODE> &d,
+                                              uint32_t rmask = ~0u)
 {
     using WT = typename WeightType<MODE>::T;
     constexpr uint32_t M2 = 0x33333333u, N1 = 0x11111111u;
     const uint32_t rup = (row + 1 == L) ? 0u : row + 1;
     const uint32_t rdn = (row == 0) ? L - 1 : row - 1;
-    d.pc = lat + (size_t)(row * WPR + q) * cpb;
+    const uint32_t rw = row & rmask;
+    d.pc = lat + (size_t)(rw * WPR + q) * cpb;
     const uint32_t C = *d.pc;
-    const uint32_t U = lat[(size_t)(rup * WPR + q) * cpb];
-    const uint32_t D = lat[(size_t)(rdn * WPR + q) * cpb];
+    const uint32_t U = lat[(size_t)((rup & rmask) * WPR + q) * cpb];
+    const uint32_t D = lat[(size_t)((rdn & rmask) * WPR + q) * cpb];
     // the one neighbour outside word q: left of the first even site, or
     // right of the last odd site (wrapping along the row)
     const uint32_t sq = half ? ((16 * q + 16 < L) ? q + 1 : 0u) : (q ? q - 1 : (L - 1) >> 4);
     const uint32_t sb = half ? 0u : (q ? 15u : ((L - 1) & 15u));
-    const uint32_t sv = spin_code(lat[(size_t)(row * WPR + sq) * cpb], sb);
+    const uint32_t sv = spin_code(lat[(size_t)(rw * WPR + sq) * cpb], sb);
 
     // Nibble t of `ctr` holds the spin code (s+1) of the window's site t;
     // nibble t of `nbs` the sum of its four neighbours' codes (0..8, no
@@ -388,10 +393,11 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
                                             ChainState &st, const uint32_t (&r1)[SLOTS], const uint32_t (&r3)[SLOTS],
                                             typename WeightType<MODE>::T eps, const float *__restrict__ btab = nullptr,
                                             uint32_t hrt = 0, const double *__restrict__ wG = nullptr,
-                                            float tol = 0.0f)
+                                            float tol = 0.0f, uint32_t rmask = ~0u)
 {
     WinDec<MODE> d;
-    decode_window<MODE, SLOTS, BT>(lat, cpb, L, WPR, row, q, HALF < 0 ? hrt : (uint32_t)HALF, r1, r3, btab, d);
+    decode_window<MODE, SLOTS, BT>(lat, cpb, L, WPR, row, q, HALF < 0 ? hrt : (uint32_t)HALF, r1, r3, btab, d,
+                                   rmask);
     // the batch kernel (the one user of the beta table) decides weight-mode
     // attempts with the one-band test
     scan_window<MODE, SLOTS, HS, BT>(d, rec, store, checked, wS, histS, histG, st, eps, wG, tol);
@@ -404,20 +410,22 @@ __device__ __noinline__ void partial_core(uint32_t *__restrict__ lat, uint32_t c
                                           uint32_t row, uint32_t q, uint32_t half, uint32_t len, bool rec,
                                           bool store, const typename WeightType<MODE>::T *__restrict__ wS,
                                           uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
-                                          ChainState &st, const uint32_t *p, const float *__restrict__ btab = nullptr)
+                                          ChainState &st, const uint32_t *p, const float *__restrict__ btab = nullptr,
+                                          uint32_t rmask = ~0u)
 {
     using WT = typename WeightType<MODE>::T;
-    const uint32_t rup = (row + 1 == L) ? 0u : row + 1;
-    const uint32_t rdn = (row == 0) ? L - 1 : row - 1;
+    const uint32_t rup = ((row + 1 == L) ? 0u : row + 1) & rmask;
+    const uint32_t rdn = ((row == 0) ? L - 1 : row - 1) & rmask;
+    const uint32_t rw = row & rmask;
     for (uint32_t t = 0; t < len; ++t) {
         const uint32_t col = 16u * q + 2u * t + half;
         const uint32_t cl = col ? col - 1 : L - 1, cr = (col + 1 == L) ? 0u : col + 1;
-        uint32_t *pw = lat + (size_t)(row * WPR + (col >> 4)) * cpb;
+        uint32_t *pw = lat + (size_t)(rw * WPR + (col >> 4)) * cpb;
         const int os = (int)spin_code(*pw, col) - 1;
         int ns = os + ((p[t] & 1u) ? -1 : 1);
         ns = ns - 3 * (ns == 2) + 3 * (ns == -2);
-        const int nb = (int)spin_code(lat[(size_t)(row * WPR + (cl >> 4)) * cpb], cl) +
-                       (int)spin_code(lat[(size_t)(row * WPR + (cr >> 4)) * cpb], cr) +
+        const int nb = (int)spin_code(lat[(size_t)(rw * WPR + (cl >> 4)) * cpb], cl) +
+                       (int)spin_code(lat[(size_t)(rw * WPR + (cr >> 4)) * cpb], cr) +
                        (int)spin_code(lat[(size_t)(rup * WPR + (col >> 4)) * cpb], col) +
                        (int)spin_code(lat[(size_t)(rdn * WPR + (col >> 4)) * cpb], col) - 4;
         const int dE = -(ns - os) * nb, dDel = ns * ns - os * os, dM = ns - os;
@@ -521,6 +529,98 @@ __device__ __forceinline__ uint32_t *prologue(const SweepArgs &a, unsigned char 
     return gl;
 }
 
+// Four-row ring of one chain's lattice in shared memory, for lattices that
+// stay in global memory.  A window of row r reads rows r - 1, r and r + 1
+// (periodic) and writes row r, so only those rows need to be near: slot
+// s = row & 3 of the ring holds row tag(s) (L is a multiple of 4, so the
+// slots follow the periodic rows).  At the start of every row the ring makes
+// rows r - 1 .. r + 1 resident (normally they already are) and starts
+// loading row r + 2 from global memory into registers, after writing the
+// slot's previous row (r - 2) back; those registers go into the slot at the
+// start of the next row, so the global latency hides behind a whole row of
+// windows.  A row that is not in its slot is not in the ring at all, so its
+// global copy is current: jumps (a new phase restarts the sweep at row 0)
+// fall back to loads at the row start.  Only the lane that owns the column
+// (`store`) moves data; padding lanes read lane 0's ring and never write.
+// WMAX >= words per row (8 for L <= 128).
+template <int WMAX>
+struct RowRing {
+    uint32_t *rs;  // the lane's ring column: word (slot, q) at rs[(slot * WPR + q) * cpb]
+    uint32_t *gs;  // the lane's global column: word (row, q) at gs[(row * WPR + q) * cpb]
+    int t0, t1, t2, t3;  // row held by each slot, -1 for none
+    int prow;            // row whose words wait in pw, -1 for none
+    uint32_t pw[WMAX];
+
+    __device__ __forceinline__ void init(uint32_t *ring_col, uint32_t *glob_col)
+    {
+        rs = ring_col;
+        gs = glob_col;
+        t0 = t1 = t2 = t3 = -1;
+        prow = -1;
+    }
+    __device__ __forceinline__ int tag(int s) const { return s == 0 ? t0 : s == 1 ? t1 : s == 2 ? t2 : t3; }
+    __device__ __forceinline__ void set_tag(int s, int v)
+    {
+        t0 = s == 0 ? v : t0;
+        t1 = s == 1 ? v : t1;
+        t2 = s == 2 ? v : t2;
+        t3 = s == 3 ? v : t3;
+    }
+    __device__ __forceinline__ void writeback(int s, uint32_t cpb, uint32_t WPR, bool store)
+    {
+        const int r = tag(s);
+        if (r < 0) return;
+        if (store)
+            for (uint32_t q = 0; q < WPR; ++q) gs[((size_t)r * WPR + q) * cpb] = rs[((size_t)s * WPR + q) * cpb];
+        set_tag(s, -1);
+    }
+    __device__ __forceinline__ void load(int row, uint32_t cpb, uint32_t WPR, bool store)
+    {
+        const int s = row & 3;
+        writeback(s, cpb, WPR, store);
+        if (store)
+            for (uint32_t q = 0; q < WPR; ++q) rs[((size_t)s * WPR + q) * cpb] = gs[((size_t)row * WPR + q) * cpb];
+        set_tag(s, row);
+    }
+    __device__ __forceinline__ void row_start(uint32_t r, uint32_t L, uint32_t cpb, uint32_t WPR, bool store)
+    {
+        if (prow >= 0) {
+            const int s = prow & 3;
+            if (store) {
+#pragma unroll
+                for (int q = 0; q < WMAX; ++q)
+                    if ((uint32_t)q < WPR) rs[((size_t)s * WPR + q) * cpb] = pw[q];
+            }
+            set_tag(s, prow);
+            prow = -1;
+        }
+        const int rm = r == 0 ? (int)L - 1 : (int)r - 1, rc = (int)r, rp = r + 1 == L ? 0 : (int)r + 1;
+        if (tag(rm & 3) != rm) load(rm, cpb, WPR, store);
+        if (tag(rc & 3) != rc) load(rc, cpb, WPR, store);
+        if (tag(rp & 3) != rp) load(rp, cpb, WPR, store);
+        const int P = rp + 1 == (int)L ? 0 : rp + 1;
+        const int s = P & 3;
+        if (tag(s) != P) {
+            writeback(s, cpb, WPR, store);
+            if (store) {
+#pragma unroll
+                for (int q = 0; q < WMAX; ++q)
+                    if ((uint32_t)q < WPR) pw[q] = gs[((size_t)P * WPR + q) * cpb];
+            }
+            prow = P;
+        }
+    }
+    __device__ __forceinline__ void finish(uint32_t cpb, uint32_t WPR, bool store)
+    {
+        for (int s = 0; s < 4; ++s) writeback(s, cpb, WPR, store);
+        prow = -1;
+    }
+};
+__host__ __device__ inline size_t ring_bytes(uint32_t L, uint32_t cpb)
+{
+    return (size_t)4 * ((L + 15) / 16) * cpb * 4;
+}
+
 template <int MODE>
 __device__ __forceinline__ void drain_hist(uint32_t *histS, unsigned long long *histG, uint32_t N)
 {
@@ -591,11 +691,15 @@ __device__ __forceinline__ bool launch_params(const SweepArgs &a, uint32_t &iter
 // hold the acceptance and direction words of the next two groups, counters
 // cc-1, cc).  Ends
 // with the block synchronised and, with HS, the shared histogram drained.
-template <int MODE, int R, bool LAT_SMEM, bool HS = true, bool BT = false>
+// RING (with LAT_SMEM false): the lattice stays in global memory and each
+// lane keeps a four-row ring of its chain in shared memory (RowRing), at the
+// offset where the whole lattice would go.
+template <int MODE, int R, bool LAT_SMEM, bool HS = true, bool BT = false, bool RING = false>
 __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned char *smem, uint32_t cpb, uint32_t blk,
                                                 uint32_t iter, unsigned long long nup,
                                                 const float *__restrict__ btab = nullptr)
 {
+    static_assert(!(RING && LAT_SMEM), "the ring serves lattices in global memory");
     using WT = typename WeightType<MODE>::T;
     const uint32_t lane = threadIdx.x;
     WT *wS;
@@ -604,6 +708,12 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
     constexpr bool DT = MODE == kModeProduce;  // production scans on the FP32 difference table
     float tol = 0.0f;
     uint32_t *lat = prologue<MODE, LAT_SMEM, HS, DT>(a, smem, lat_off, cpb, lane, blk, wS, histS, gl, &tol);
+    RowRing<8> ring;
+    if (RING) {
+        ring.init(reinterpret_cast<uint32_t *>(smem + lat_off) + (lane < cpb ? lane : 0u), gl);
+        lat = ring.rs;
+    }
+    constexpr uint32_t rmask = RING ? 3u : ~0u;
     __syncthreads();
     const double *wG = reinterpret_cast<const double *>(a.w);
     // the step-by-step path reads the weights it needs: FP64 ones from global memory in production
@@ -642,11 +752,13 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
     for_each_window(L, WPR, a.therm, nup, [&](uint32_t row, uint32_t q, uint32_t half, uint32_t cnt, uint32_t len,
                                               bool rec_phase) {
         const bool rec = rec_phase && cs.active;
+        if (RING && q == 0) ring.row_start(row, L, cpb, WPR, store);
         if (len < cnt) {
             uint32_t p[8];
 #pragma unroll
             for (int t = 0; t < 8; ++t) p[t] = pack_draw(n1[t], n3[t]);
-            partial_core<MODE, HS, BT>(lat, cpb, L, WPR, row, q, half, len, rec, store, wP, histS, a.hist, st, p, btab);
+            partial_core<MODE, HS, BT>(lat, cpb, L, WPR, row, q, half, len, rec, store, wP, histS, a.hist, st, p, btab,
+                                       rmask);
             advance((len + 3u) >> 2);
         } else if (cnt == 8) {
             uint32_t r1[8], r3[8];
@@ -657,7 +769,7 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
             }
             advance(2);  // independent of the window below: overlaps its scan
             window_core<MODE, 8, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
-                                             r3, eps, btab, half, wG, tol);
+                                             r3, eps, btab, half, wG, tol, rmask);
         } else {
             uint32_t r1[4], r3[4];
 #pragma unroll
@@ -667,7 +779,7 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
             }
             advance(1);
             window_core<MODE, 4, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
-                                             r3, eps, btab, half, wG, tol);
+                                             r3, eps, btab, half, wG, tol, rmask);
         }
         return true;
     });
@@ -675,6 +787,7 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
         const uint32_t words = L * WPR;
         for (uint32_t w = 0; w < words; ++w) gl[(size_t)w * cpb] = lat[(size_t)w * cpb];
     }
+    if (RING) ring.finish(cpb, WPR, store);
     if (cs.active) {
         a.edel[cs.chain] = st.E;
         a.ej[cs.chain] = st.EJ;

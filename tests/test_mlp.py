@@ -50,10 +50,11 @@ def test_param_count_and_features():
 
 
 @pytest.mark.gpu
-def test_forward_and_gradient_vs_reference(muca):
+@pytest.mark.parametrize("n", [1000, 999, 33, 4096])
+def test_forward_and_gradient_vs_reference(muca, n):
     rng = np.random.default_rng(2)
     p = _init(2).astype(np.float32)
-    x, t = _points(rng, 1000)  # not a multiple of the 32-point tile
+    x, t = _points(rng, n)  # 1000, 999, 33: not multiples of the 32-point tile; odd sizes shift the scratch
     with muca.MLP(seed=5) as net:
         net.set_params(p)
         y = net.predict(x)
