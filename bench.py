@@ -76,6 +76,7 @@ def parse():
     p.add_argument("--blocks", type=int, default=10, help="jackknife blocks of --only production")
     p.add_argument("--block-sweeps", type=int, default=100, help="production sweeps per block of --only production")
     p.add_argument("--therm-sweeps", type=int, default=100, help="thermalisation sweeps of --only production")
+    p.add_argument("--mlp-steps", type=int, default=2048, help="timed training steps of --only mlp")
     p.add_argument("--state-out", default=None, help="--only production: save the converged weight and lattices")
     p.add_argument("--state-in", default=None, help="--only production: start from a saved state (no weight run)")
     p.add_argument("--kernel", type=int, default=0, help="sweep kernel: 0 auto, 1 generic, 2 windowed, 3 specialised")
@@ -855,7 +856,8 @@ def main():
         from muca_gb300 import build as b
         b.build()
         fn = {"flat_run": flat_run_metric, "config2": config2_metric, "batch": batch_metric,
-              "random_site": random_site_metric, "warm_start": warm_start_metric, "mlp": mlp_metric,
+              "random_site": random_site_metric, "warm_start": warm_start_metric,
+              "mlp": lambda d: mlp_metric(d, steps=args.mlp_steps),
               "production": lambda d: production_metric(d, args.production_L, with_ref=False, kernel=args.kernel,
                                                         blocks=args.blocks, block_sweeps=args.block_sweeps,
                                                         therm_sweeps=args.therm_sweeps,

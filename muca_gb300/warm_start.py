@@ -27,10 +27,12 @@ import numpy as np
 import muca_gb300 as m
 
 # the weight iteration used for the training data and both arms of the A/B
-# (schedule 5: NUPDATES held until the width is N, then x1.05 per iteration;
-# one schedule for every arm)
-RUN_OPTS = dict(starting_M=1, rule=m.UPDATE_TRIVIAL, nup_schedule=5, flat_minmean=1, max_iter=20000,
-                graph_iters=32, starting_sweeps=1, nup_max=1 << 20)
+# (schedule 4, the CPU program's NUPDATES x1.05 from the first iteration,
+# capped at 2^16 per chain; one schedule for every arm of an A/B)
+RUN_OPTS = dict(starting_M=1, rule=m.UPDATE_TRIVIAL, nup_schedule=4, flat_minmean=1, max_iter=20000,
+                graph_iters=32, starting_sweeps=1, nup_max=1 << 16)
+# the training data: NUPDATES doubling once the width is N (capped at 2^16)
+DATA_OPTS = dict(RUN_OPTS, nup_schedule=1)
 
 
 def converge(instances, opts=RUN_OPTS, warm=None, device=0):
@@ -146,10 +148,6 @@ def ab_test(net, held, opts=RUN_OPTS, device=0, sources=None, graded=False):
         arms["interp"] = [interpolated_weight(L, T, sources) for L, _, T, _, _ in held]
     rz, sz, wz = converge(held, opts, None, device)
     runs = {k: converge(held, opts, w, device) for k, w in arms.items()}
-    # the statistical floor of the final weights: the zero weight again with other seeds
-    runs["zero_reseeded"] = converge([(L, nc, T, D, seed + 7919) for L, nc, T, D, seed in held], opts, None,
-                                     device)
-    arms["zero_reseeded"] = [np.zeros_like(w) for w in wz]
     if graded:
         og = dict(opts, reinit_chains=1, graded_init=1)
         runs["zero_g"] = converge(held, og, None, device)
@@ -232,54 +230,73 @@ def held_out_instances(Ls, Ts, rng, chains):
 
 
 def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, held_T=(0.43, 0.53, 0.63, 0.73),
-              held_L=(), schedule=5, steps=10000, device=0, reference_criterion=True, graded=False,
-              ab_schedules=()):
-    """The whole study: training data from the batched engine (every (L, T)
-    on the grid, seed per instance), the network trained on the device, the
-    A/B on the held-out (L, T, Delta) to min/mean >= 0.5 with one NUPDATES
-    schedule for every arm, and (reference_criterion) the same arms run to
-    the reference's criterion (width == N and D_KL < 1e-4) for the
-    agreement of the final weights."""
+              held_L=(), schedule=4, steps=10000, device=0, reference_criterion=True, agreement_Lmax=48,
+              graded=False, ab_schedules=(), save=None, load=None):
+    """The study: training data from the batched engine (every (L, T) on the
+    grid, a seed per instance, DATA_OPTS), the network trained on the
+    device, the A/B on the held-out (L, T, Delta) to min/mean >= 0.5 with one
+    NUPDATES schedule for every arm (`schedule`, capped at 2^16), and
+    (reference_criterion) the arms run to the reference's criterion
+    (width == N and D_KL < 1e-4) on the held-out instances of L <=
+    agreement_Lmax, for the agreement of the final weights.  `save` writes
+    the training set, converged training weights and network parameters to
+    an .npz; `load` reads them back instead of generating and training."""
     t_all = time.time()
-    Ts = np.round(np.arange(0.40, 0.8 + 1e-9, t_step), 4)
     rng = np.random.default_rng(0)
     opts = dict(RUN_OPTS, nup_schedule=schedule)
-    train_inst = [(L, chains, float(T), float(rng.uniform(1.5, 1.99)), 1000 + k)
-                  for k, (L, T) in enumerate([(L, T) for L in Ls for T in Ts])]
-    t0 = time.time()
-    res, sec, W = converge(train_inst, opts, None, device)
-    ok = [i for i, r in enumerate(res) if r.converged]
-    x, t = training_set([train_inst[i] for i in ok], [W[i] for i in ok])
-    gen = {"instances": len(train_inst), "sizes": list(Ls), "chains": chains, "converged": len(ok),
-           "device_s": sec, "wall_s": time.time() - t0,
-           "iters_median": float(np.median([r.iterations for r in res])),
-           "iters_max": int(max(r.iterations for r in res)), "points": int(x.shape[0])}
-    out = {"run_opts": dict(opts), "training_set": gen}
+    out = {"run_opts": dict(opts), "data_opts": dict(DATA_OPTS)}
     with m.MLP(device=device, seed=7) as net:
-        t0 = time.time()
-        sched = ((steps, 1e-3), (steps, 3e-4), (steps, 1e-4))
-        losses = train(net, x, t, schedule=sched)
-        fit_s = time.time() - t0
-        flops = 3 * losses.size * 4096 * 2 * net.n_params  # forward + backward: ~3 x 2 flop per weight and point
-        out["fit"] = {"steps": int(losses.size), "batch": 4096, "lr": [s_[1] for s_ in sched],
-                      "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
-                      "wall_s": fit_s, "tflops": flops / fit_s / 1e12}
+        if load:
+            z = np.load(load, allow_pickle=False)
+            net.set_params(z["params"])
+            src_meta = z["src_meta"]
+            src_w = [z["src_w_%d" % i] for i in range(len(src_meta))]
+            sources = [(int(Lm), float(Tm), w) for (Lm, Tm), w in zip(src_meta, src_w)]
+            for _ in range(len(Ls) * len(np.arange(0.40, 0.8 + 1e-9, t_step))):
+                rng.uniform(1.5, 1.99)  # the same held-out Deltas as the generating run
+            out["training_set"] = {"loaded": load, "sources": len(sources)}
+        else:
+            Ts = np.round(np.arange(0.40, 0.8 + 1e-9, t_step), 4)
+            train_inst = [(L, chains, float(T), float(rng.uniform(1.5, 1.99)), 1000 + k)
+                          for k, (L, T) in enumerate([(L, T) for L in Ls for T in Ts])]
+            t0 = time.time()
+            res, sec, W = converge(train_inst, DATA_OPTS, None, device)
+            ok = [i for i, r in enumerate(res) if r.converged]
+            x, t = training_set([train_inst[i] for i in ok], [W[i] for i in ok])
+            out["training_set"] = {"instances": len(train_inst), "sizes": list(Ls), "chains": chains,
+                                   "converged": len(ok), "device_s": sec, "wall_s": time.time() - t0,
+                                   "iters_median": float(np.median([r.iterations for r in res])),
+                                   "iters_max": int(max(r.iterations for r in res)), "points": int(x.shape[0])}
+            t0 = time.time()
+            sched = ((steps, 1e-3), (steps, 3e-4), (steps, 1e-4))
+            losses = train(net, x, t, schedule=sched)
+            fit_s = time.time() - t0
+            flops = 6.0 * losses.size * 4096 * net.n_params  # forward + two backward products
+            out["fit"] = {"steps": int(losses.size), "batch": 4096, "lr": [s_[1] for s_ in sched],
+                          "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
+                          "wall_s": fit_s, "tflops": flops / fit_s / 1e12}
+            sources = [(train_inst[i][0], train_inst[i][2], W[i]) for i in ok]
+            if save:
+                arrs = {"params": net.params(),
+                        "src_meta": np.array([(Lm, Tm) for Lm, Tm, _ in sources], np.float64)}
+                arrs.update({"src_w_%d" % i: w for i, (_, _, w) in enumerate(sources)})
+                np.savez(save, **arrs)
         held = held_out_instances(list(Ls) + list(held_L), held_T, rng, chains)
-        sources = [(train_inst[i][0], train_inst[i][2], W[i]) for i in ok]
         t0 = time.time()
         ab = ab_test(net, held, opts, device, sources, graded=graded)
         ab["wall_s"] = time.time() - t0
         out["ab"] = ab
         if reference_criterion:
-            ro = dict(opts, flat_minmean=0, max_iter=40000)
+            sub = [h for h in held if h[0] <= agreement_Lmax]
+            ro = dict(opts, flat_minmean=0, max_iter=40000, nup_max=1 << 18)
             t0 = time.time()
-            out["agreement_reference_criterion"] = agreement_under(net, held, sources, ro, device)
-            out["agreement_reference_criterion"]["wall_s"] = time.time() - t0
-        # the A/B under other NUPDATES schedules (the same network; every arm
-        # alike); NUPDATES capped at 2^16 there, which keeps schedule 4's
-        # zero arm (x1.05 from the first iteration, through thousands of
-        # width-growing iterations at L = 128) within minutes
-        ab_sched = {int(sc): ab_test(net, held, dict(opts, nup_schedule=int(sc), nup_max=1 << 16), device, sources)
+            ag = agreement_under(net, sub, sources, ro, device)
+            ag["wall_s"] = time.time() - t0
+            ag["instances"] = [(L, T) for L, _, T, _, _ in sub]
+            ag["run_opts"] = ro
+            out["agreement_reference_criterion"] = ag
+        # the A/B under other NUPDATES schedules (the same network; every arm alike)
+        ab_sched = {int(sc): ab_test(net, held, dict(opts, nup_schedule=int(sc)), device, sources)
                     for sc in ab_schedules}
         if ab_sched:
             out["ab_schedules"] = ab_sched
@@ -296,7 +313,11 @@ def main(argv=None):
     p.add_argument("--held-L", default="", help="held-out lattice sizes beyond the training ones")
     p.add_argument("--graded", action="store_true", help="also run the arms from graded initial spins")
     p.add_argument("--steps", type=int, default=10000, help="Adam steps per learning-rate stage (3 stages)")
-    p.add_argument("--schedule", type=int, default=5, help="NUPDATES schedule of every arm")
+    p.add_argument("--schedule", type=int, default=4, help="NUPDATES schedule of every arm")
+    p.add_argument("--agreement-Lmax", type=int, default=48,
+                   help="largest L of the held-out instances run to the reference criterion")
+    p.add_argument("--save", default=None, help="write the training set's weights and the network to this .npz")
+    p.add_argument("--load", default=None, help="read them from this .npz instead of generating and training")
     p.add_argument("--ab-schedules", default="",
                    help="NUPDATES schedules to repeat the A/B with (same network), e.g. 0,4")
     p.add_argument("--no-reference-criterion", action="store_true",
@@ -306,8 +327,9 @@ def main(argv=None):
     out = run_study(Ls=[int(v) for v in a.L.split(",")], chains=a.chains, t_step=a.t_step,
                     held_T=[float(v) for v in a.held_T.split(",")],
                     held_L=[int(v) for v in a.held_L.split(",") if v], schedule=a.schedule, steps=a.steps,
-                    device=a.device, reference_criterion=not a.no_reference_criterion, graded=a.graded,
-                    ab_schedules=[int(v) for v in a.ab_schedules.split(",") if v])
+                    device=a.device, reference_criterion=not a.no_reference_criterion,
+                    agreement_Lmax=a.agreement_Lmax, graded=a.graded,
+                    ab_schedules=[int(v) for v in a.ab_schedules.split(",") if v], save=a.save, load=a.load)
     print(json.dumps(out))
     return out
 

@@ -3,8 +3,8 @@ the batched engine train the MLP on the device; on held-out (L, T) the weight
 iteration from the network's prediction reaches the same flat-histogram
 criterion (min/mean >= 0.5) in at least 3x fewer iterations and in less
 device time than from the zero weight, with the same seeds, options and
-NUPDATES schedule for every arm (schedule 5: held until full width, then
-x1.05 per iteration).  The two non-learned arms (the reference's
+NUPDATES schedule for every arm (schedule 4, the CPU program's x1.05 per
+iteration, capped at 2^16).  The two non-learned arms (the reference's
 piecewise-linear form and the full weights, interpolated in T) run beside it
 and converge."""
 import numpy as np
