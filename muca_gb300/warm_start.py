@@ -231,7 +231,7 @@ def held_out_instances(Ls, Ts, rng, chains):
 
 def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, held_T=(0.43, 0.53, 0.63, 0.73),
               held_L=(), schedule=4, steps=10000, device=0, reference_criterion=True, agreement_Lmax=48,
-              graded=False, ab_schedules=(), save=None, load=None):
+              graded=False, ab_schedules=(), save=None, load=None, progress=None):
     """The study: training data from the batched engine (every (L, T) on the
     grid, a seed per instance, DATA_OPTS), the network trained on the
     device, the A/B on the held-out (L, T, Delta) to min/mean >= 0.5 with one
@@ -240,8 +240,15 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
     (width == N and D_KL < 1e-4) on the held-out instances of L <=
     agreement_Lmax, for the agreement of the final weights.  `save` writes
     the training set, converged training weights and network parameters to
-    an .npz; `load` reads them back instead of generating and training."""
+    an .npz; `load` reads them back instead of generating and training.
+    `progress`: a JSON file rewritten with the results so far after every
+    stage."""
     t_all = time.time()
+
+    def dump(o):
+        if progress:
+            with open(progress, "w") as f:
+                json.dump(o, f)
     rng = np.random.default_rng(0)
     opts = dict(RUN_OPTS, nup_schedule=schedule)
     out = {"run_opts": dict(opts), "data_opts": dict(DATA_OPTS)}
@@ -281,11 +288,13 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
                         "src_meta": np.array([(Lm, Tm) for Lm, Tm, _ in sources], np.float64)}
                 arrs.update({"src_w_%d" % i: w for i, (_, _, w) in enumerate(sources)})
                 np.savez(save, **arrs)
+        dump(out)
         held = held_out_instances(list(Ls) + list(held_L), held_T, rng, chains)
         t0 = time.time()
         ab = ab_test(net, held, opts, device, sources, graded=graded)
         ab["wall_s"] = time.time() - t0
         out["ab"] = ab
+        dump(out)
         if reference_criterion:
             sub = [h for h in held if h[0] <= agreement_Lmax]
             ro = dict(opts, flat_minmean=0, max_iter=40000, nup_max=1 << 18)
@@ -295,11 +304,13 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
             ag["instances"] = [(L, T) for L, _, T, _, _ in sub]
             ag["run_opts"] = ro
             out["agreement_reference_criterion"] = ag
+            dump(out)
         # the A/B under other NUPDATES schedules (the same network; every arm alike)
-        ab_sched = {int(sc): ab_test(net, held, dict(opts, nup_schedule=int(sc)), device, sources)
-                    for sc in ab_schedules}
-        if ab_sched:
+        ab_sched = {}
+        for sc in ab_schedules:
+            ab_sched[int(sc)] = ab_test(net, held, dict(opts, nup_schedule=int(sc)), device, sources)
             out["ab_schedules"] = ab_sched
+            dump(out)
     out["wall_s"] = time.time() - t_all
     return out
 
@@ -318,6 +329,7 @@ def main(argv=None):
                    help="largest L of the held-out instances run to the reference criterion")
     p.add_argument("--save", default=None, help="write the training set's weights and the network to this .npz")
     p.add_argument("--load", default=None, help="read them from this .npz instead of generating and training")
+    p.add_argument("--progress", default=None, help="JSON file rewritten with the results so far after every stage")
     p.add_argument("--ab-schedules", default="",
                    help="NUPDATES schedules to repeat the A/B with (same network), e.g. 0,4")
     p.add_argument("--no-reference-criterion", action="store_true",
@@ -329,7 +341,8 @@ def main(argv=None):
                     held_L=[int(v) for v in a.held_L.split(",") if v], schedule=a.schedule, steps=a.steps,
                     device=a.device, reference_criterion=not a.no_reference_criterion,
                     agreement_Lmax=a.agreement_Lmax, graded=a.graded,
-                    ab_schedules=[int(v) for v in a.ab_schedules.split(",") if v], save=a.save, load=a.load)
+                    ab_schedules=[int(v) for v in a.ab_schedules.split(",") if v], save=a.save, load=a.load,
+                    progress=a.progress)
     print(json.dumps(out))
     return out
 
