@@ -231,7 +231,8 @@ def held_out_instances(Ls, Ts, rng, chains):
 
 def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, held_T=(0.43, 0.53, 0.63, 0.73),
               held_L=(), schedule=4, steps=10000, device=0, reference_criterion=True, agreement_Lmax=48,
-              graded=False, ab_schedules=(), save=None, load=None, progress=None):
+              graded=False, ab_schedules=(), save=None, load=None, progress=None, held_sizes=None, nup_max=None,
+              max_iter=None):
     """The study: training data from the batched engine (every (L, T) on the
     grid, a seed per instance, DATA_OPTS), the network trained on the
     device, the A/B on the held-out (L, T, Delta) to min/mean >= 0.5 with one
@@ -242,7 +243,8 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
     the training set, converged training weights and network parameters to
     an .npz; `load` reads them back instead of generating and training.
     `progress`: a JSON file rewritten with the results so far after every
-    stage."""
+    stage.  held_sizes: run the A/B only on the held-out instances of these
+    sizes; nup_max / max_iter: the A/B's NUPDATES cap and iteration cap."""
     t_all = time.time()
 
     def dump(o):
@@ -251,6 +253,10 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
                 json.dump(o, f)
     rng = np.random.default_rng(0)
     opts = dict(RUN_OPTS, nup_schedule=schedule)
+    if nup_max:
+        opts["nup_max"] = nup_max
+    if max_iter:
+        opts["max_iter"] = max_iter
     out = {"run_opts": dict(opts), "data_opts": dict(DATA_OPTS)}
     with m.MLP(device=device, seed=7) as net:
         if load:
@@ -290,6 +296,8 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
                 np.savez(save, **arrs)
         dump(out)
         held = held_out_instances(list(Ls) + list(held_L), held_T, rng, chains)
+        if held_sizes:
+            held = [h for h in held if h[0] in held_sizes]
         t0 = time.time()
         ab = ab_test(net, held, opts, device, sources, graded=graded)
         ab["wall_s"] = time.time() - t0
@@ -330,6 +338,9 @@ def main(argv=None):
     p.add_argument("--save", default=None, help="write the training set's weights and the network to this .npz")
     p.add_argument("--load", default=None, help="read them from this .npz instead of generating and training")
     p.add_argument("--progress", default=None, help="JSON file rewritten with the results so far after every stage")
+    p.add_argument("--held-sizes", default="", help="run the A/B only on the held-out instances of these sizes")
+    p.add_argument("--nup-max", type=int, default=0, help="NUPDATES cap of the A/B (0: RUN_OPTS')")
+    p.add_argument("--max-iter", type=int, default=0, help="iteration cap of the A/B (0: RUN_OPTS')")
     p.add_argument("--ab-schedules", default="",
                    help="NUPDATES schedules to repeat the A/B with (same network), e.g. 0,4")
     p.add_argument("--no-reference-criterion", action="store_true",
@@ -342,7 +353,8 @@ def main(argv=None):
                     device=a.device, reference_criterion=not a.no_reference_criterion,
                     agreement_Lmax=a.agreement_Lmax, graded=a.graded,
                     ab_schedules=[int(v) for v in a.ab_schedules.split(",") if v], save=a.save, load=a.load,
-                    progress=a.progress)
+                    progress=a.progress, held_sizes=[int(v) for v in a.held_sizes.split(",") if v],
+                    nup_max=a.nup_max or None, max_iter=a.max_iter or None)
     print(json.dumps(out))
     return out
 
