@@ -28,10 +28,10 @@ import muca_gb300 as m
 
 # the weight iteration used for the training data and both arms of the A/B
 # (schedule 4, the CPU program's NUPDATES x1.05 from the first iteration,
-# capped at 2^16 per chain; one schedule for every arm of an A/B)
+# capped at 2^18 per chain; one schedule for every arm of an A/B)
 RUN_OPTS = dict(starting_M=1, rule=m.UPDATE_TRIVIAL, nup_schedule=4, flat_minmean=1, max_iter=20000,
-                graph_iters=32, starting_sweeps=1, nup_max=1 << 16)
-# the training data: NUPDATES doubling once the width is N (capped at 2^16)
+                graph_iters=32, starting_sweeps=1, nup_max=1 << 18)
+# the training data: NUPDATES doubling once the width is N (capped at 2^18)
 DATA_OPTS = dict(RUN_OPTS, nup_schedule=1)
 
 
