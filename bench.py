@@ -27,10 +27,16 @@ weight update on the device.  Spins start from the reference initialisation
                 chain per thread task, all host threads) on full steps.
 
 Beside the headline the default line carries `flat_run` (iterations and time
-to a flat histogram), `batch` (256 uneven instances), `production` (L=128
-with its reweighting) and `random_site` (the CPU weight program's algorithm
-on the device, with the oracle's restatement of it on the host threads);
-`--only NAME` prints one of them alone.
+to a flat histogram), `config2` (the L=72 configuration as written: runs
+from starting_M = 1, the recursion, steps from converged weights, the
+reference's own chain count), `batch` (256 uneven instances), `production`
+(the L=128 configuration: a converged weight, jackknifed <|M|>, chi and U4
+over 10 blocks, the reweighting, and the reference's CPU production
+algorithm on the host threads) and `random_site` (the CPU weight program's
+algorithm on the device, with the oracle's restatement of it on the host
+threads); `--only NAME` prints one of them alone.  `--only warm_start` (the
+learned warm start's study, minutes of GPU time) and `--only mlp` (the
+network's training throughput) are not part of the default line.
 
 `--impl reference` times the reference's CPU algorithm (the oracle port: the
 reference CPU sources cannot be built on the GPU host) on the same workload.
