@@ -144,6 +144,75 @@ inline void die_io(const std::string &why)
     std::exit(3);
 }
 
+// Chain files (no reference counterpart: the reference saves no lattice,
+// and produce_gpu always starts from fresh random spins,
+// produce2_multigpu.cu:126-140).  A weight run's final lattices can start a
+// production run, so that the chains begin where the converged
+// multicanonical walk left them, spread over E_Delta, instead of all near
+// E_Delta = 2N/3.  Format: the 8 bytes "MUCACHN1", u32 L, u32 chains (little
+// endian), then chains * L * L int8 spins in {-1, 0, +1}, [chain][site],
+// site = row * L + col.
+inline bool write_chains(const std::string &path, uint32_t L, uint32_t chains, const std::vector<int8_t> &lat,
+                         std::string &why)
+{
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) {
+        why = path + ": cannot create";
+        return false;
+    }
+    const uint32_t hdr[2] = {L, chains};
+    bool ok = std::fwrite("MUCACHN1", 1, 8, f) == 8 && std::fwrite(hdr, 4, 2, f) == 2 &&
+              std::fwrite(lat.data(), 1, lat.size(), f) == lat.size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) why = path + ": write failed";
+    return ok;
+}
+
+inline bool read_chains(const std::string &path, uint32_t L, uint32_t chains, std::vector<int8_t> &lat,
+                        std::string &why)
+{
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) {
+        why = path + ": cannot open";
+        return false;
+    }
+    char magic[8];
+    uint32_t hdr[2] = {0, 0};
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "MUCACHN1", 8) == 0 && std::fread(hdr, 4, 2, f) == 2;
+    if (!ok) {
+        std::fclose(f);
+        why = path + ": not a chain file";
+        return false;
+    }
+    if (hdr[0] != L || hdr[1] != chains) {
+        std::fclose(f);
+        why = path + ": holds " + std::to_string(hdr[1]) + " chains of L=" + std::to_string(hdr[0]) + ", expected " +
+              std::to_string(chains) + " of L=" + std::to_string(L);
+        return false;
+    }
+    lat.assign((size_t)chains * L * L, 0);
+    ok = std::fread(lat.data(), 1, lat.size(), f) == lat.size();
+    char extra;
+    const bool trailing = std::fread(&extra, 1, 1, f) == 1;
+    std::fclose(f);
+    if (!ok || trailing) {
+        why = path + ": " + (ok ? "trailing bytes" : "truncated");
+        return false;
+    }
+    for (size_t i = 0; i < lat.size(); ++i)
+        if (lat[i] < -1 || lat[i] > 1) {
+            why = path + ": spin " + std::to_string(i) + " is " + std::to_string((int)lat[i]) + ", not in {-1, 0, 1}";
+            return false;
+        }
+    return true;
+}
+
+inline void die_chains(const std::string &why)
+{
+    std::fprintf(stderr, "error: chain file: %s\n", why.c_str());
+    std::exit(3);
+}
+
 // ./fss/L<L> is where the reference programs read and write their files.
 inline void ensure_dir(const std::string &d)
 {

@@ -64,7 +64,8 @@ int main(int argc, char **argv)
     if (pos.size() < 7) {
         std::fprintf(stderr,
                      "usage: %s L starting_gpu last_gpu jacks starting_M recursive_update continuing [rand_config]\n"
-                     "          [--device=D] [--chains=NW] [--max-iter=K] [--flat=minmean] [--kernel=0..3]\n",
+                     "          [--device=D] [--chains=NW] [--max-iter=K] [--flat=minmean] [--kernel=0..3]\n"
+                     "          [--save-chains=FILE]\n",
                      argv[0]);
         return 2;
     }
@@ -188,6 +189,14 @@ int main(int argc, char **argv)
         } else {
             std::cout << "Noooo...not converged";
         }
+    }
+
+    // --save-chains: the chains' final lattices, for a production run to start from
+    if (opt.has("save-chains")) {
+        std::vector<int8_t> lat((size_t)NUM_WORKERS * NofGPU * N);
+        if (muca_get_lattice(ctx, lat.data(), lat.size()) != MUCA_OK) cli::die("get lattice", ctx);
+        std::string why;
+        if (!cli::write_chains(opt.str("save-chains", ""), L, NUM_WORKERS * NofGPU, lat, why)) cli::die_chains(why);
     }
 
     // jackknife of the timings and step counts (:498-507), on the device

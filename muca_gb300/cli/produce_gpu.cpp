@@ -28,6 +28,10 @@
 //                  histogram(s) with its own shifted weights: `range` times
 //                  fewer sweeps.  The first line equals the one without the
 //                  option;
+//   --load-chains=FILE  start the chains from a chain file written by
+//                  multigpu_weight --save-chains (the weight run's final
+//                  lattices, spread over E_Delta by the converged walk)
+//                  instead of fresh random spins (:126-140);
 //   ./fss/L<L> is created when missing.
 #include <fstream>
 #include <iomanip>
@@ -45,7 +49,7 @@ int main(int argc, char **argv)
         std::fprintf(stderr,
                      "usage: %s L first_gpu last_gpu range jacks therm_mult nup_mult delta gap\n"
                      "          [--device=D] [--chains=NW] [--jack-blocks] [--binder] [--reuse-histogram]\n"
-                     "          [--kernel=0..3]\n",
+                     "          [--kernel=0..3] [--load-chains=FILE]\n",
                      argv[0]);
         return 2;
     }
@@ -79,6 +83,15 @@ int main(int argc, char **argv)
     } else if (muca_default_chains(device, &NUM_WORKERS) != MUCA_OK) {
         cli::die("device query", nullptr);
     }
+    // --load-chains: start every device's chains from a weight run's final
+    // lattices (device g takes chains g*NW .. g*NW + NW - 1), checked before
+    // any device work
+    std::vector<int8_t> start_lat;
+    if (opt.has("load-chains")) {
+        std::string why;
+        if (!cli::read_chains(opt.str("load-chains", ""), L, NUM_WORKERS * NofGPU, start_lat, why))
+            cli::die_chains(why);
+    }
 
     // one context per emulated device: each has its own 2D histogram
     std::vector<muca_ctx *> ctx(NofGPU, nullptr);
@@ -94,6 +107,9 @@ int main(int argc, char **argv)
         prm.kernel = (uint32_t)opt.num("kernel", 0);
         if (muca_create(&prm, &ctx[g]) != MUCA_OK) cli::die("create", nullptr);
         if (muca_init_chains(ctx[g], MUCA_INIT_PRODUCE, 0) != MUCA_OK) cli::die("init chains", ctx[g]);
+        if (!start_lat.empty() &&
+            muca_set_lattice(ctx[g], start_lat.data() + (size_t)g * NUM_WORKERS * N, (size_t)NUM_WORKERS * N) != MUCA_OK)
+            cli::die("set lattice", ctx[g]);
     }
     cli::ensure_dir("./fss/L" + Ls);
 

@@ -93,18 +93,24 @@ def _produce_restated(orc, L, NW, ndev, rng_, tm, nm, delta0, gap, lnw_file):
     return [(m, s) for m, s, _ in _produce_variants(orc, L, NW, ndev, rng_, 0, tm, nm, delta0, gap, lnw_file)]
 
 
-def _produce_variants(orc, L, NW, ndev, rng_, jacks, tm, nm, delta0, gap, lnw_file, blocks=False, reuse=False):
+def _produce_variants(orc, L, NW, ndev, rng_, jacks, tm, nm, delta0, gap, lnw_file, blocks=False, reuse=False,
+                      start_lats=None):
     """The production loop with the options of produce_gpu: `blocks`
     jackknifes over `jacks` production blocks (seeds of the block loop at
     produce2_multigpu.cu:324-347, iter jj, seed 100 + l + 2000 g), `reuse`
     runs the thermalisation and production of the first Delta point only and
     reweights its histograms at every point.  Returns per Delta point the
-    jackknifed (<|M|>, chi, U4) as (avg, err) pairs."""
+    jackknifed (<|M|>, chi, U4) as (avg, err) pairs.  `start_lats`
+    ([chain][site], NW * ndev chains): the chains start there (--load-chains)
+    instead of from the reference's initial spins."""
     N = L * L
     beta = 2.0
     lats, ejs, eds, mgs = [], [], [], []
     for g in range(ndev):
-        lat = orc.init_lattice(L, NW, orc.scheme_produce(g)).copy()
+        if start_lats is not None:
+            lat = np.ascontiguousarray(start_lats[g * NW:(g + 1) * NW], np.int8).copy()
+        else:
+            lat = orc.init_lattice(L, NW, orc.scheme_produce(g)).copy()
         ej, ed, mg = orc.energies(L, lat)
         lats.append(lat); ejs.append(ej); eds.append(ed); mgs.append(mg)
     deltas, d = [], delta0
@@ -359,3 +365,85 @@ def test_multigpu_weight_rejects_malformed_initial_weight(exes, tmp_path, case):
     assert r.returncode == 3, (r.returncode, r.stderr)
     expect = {"truncated": "16 values, expected N+1 = 17", "non_numeric": "'x1'", "missing": "cannot open"}[case]
     assert expect in r.stderr, r.stderr
+
+
+# ---- chain files: production from a weight run's final lattices --------------------------------
+
+def _chain_file(path, L, n, lat=None, magic=b"MUCACHN1", extra=b""):
+    import struct
+    if lat is None:
+        lat = np.zeros((n, L * L), np.int8)
+    with open(path, "wb") as f:
+        f.write(magic + struct.pack("<II", L, n) + np.ascontiguousarray(lat, np.int8).tobytes() + extra)
+
+
+def _read_chain_file(path):
+    import struct
+    b = open(path, "rb").read()
+    assert b[:8] == b"MUCACHN1"
+    L, n = struct.unpack("<II", b[8:16])
+    lat = np.frombuffer(b[16:], np.int8).reshape(n, L * L)
+    return L, n, lat
+
+
+@pytest.mark.parametrize("case", ["missing", "magic", "size", "truncated", "spin"])
+def test_produce_gpu_rejects_bad_chain_file(exes, tmp_path, case):
+    """--load-chains is checked before any device work (no GPU needed): the
+    file must hold exactly chains x N spins in {-1, 0, 1} for this L and
+    chain count, after the header."""
+    L, NW = 4, 64
+    N = L * L
+    d = tmp_path / "fss" / ("L%d" % L)
+    d.mkdir(parents=True)
+    (d / "weight_mpi_T050c16_M200_JACK0_DKL1e-4.txt").write_text(_weight_pairs(L, -0.5 * np.arange(N + 1)))
+    cf = tmp_path / "chains.bin"
+    if case == "magic":
+        _chain_file(cf, L, NW, magic=b"NOTCHAIN")
+    elif case == "size":
+        _chain_file(cf, L, NW + 1)
+    elif case == "truncated":
+        _chain_file(cf, L, NW)
+        cf.write_bytes(cf.read_bytes()[:-5])
+    elif case == "spin":
+        lat = np.zeros((NW, N), np.int8)
+        lat[3, 7] = 2
+        _chain_file(cf, L, NW, lat)
+    args = [str(L), "0", "0", "1", "1", "1", "1", "1.9", "0.1", "--chains=%d" % NW, "--load-chains=%s" % cf]
+    r = subprocess.run([exes[1]] + args, capture_output=True, text=True, cwd=tmp_path, timeout=120)
+    assert r.returncode == 3, (r.returncode, r.stderr)
+    expect = {"missing": "cannot open", "magic": "not a chain file", "size": "expected 64 of L=4",
+              "truncated": "truncated", "spin": "not in {-1, 0, 1}"}[case]
+    assert "chain file" in r.stderr and expect in r.stderr, r.stderr
+
+
+@pytest.mark.gpu
+def test_weight_run_chains_start_production(exes, orc, tmp_path):
+    """multigpu_weight --save-chains writes the chains' final lattices;
+    produce_gpu --load-chains starts from them.  The observables equal the
+    reference production loop restated with the oracle from those lattices."""
+    L, NW, jacks, rng_, tm, nm = 8, 128, 4, 2, 5, 20
+    N = L * L
+    cf = tmp_path / "chains.bin"
+    r = subprocess.run([exes[0], str(L), "0", "0", "1", "64", "0", "0", "--chains=%d" % NW, "--flat=minmean",
+                        "--max-iter=3000", "--save-chains=%s" % cf], capture_output=True, text=True, cwd=tmp_path,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    Lc, n, lat = _read_chain_file(cf)
+    assert (Lc, n) == (L, NW) and set(np.unique(lat)) <= {-1, 0, 1}
+    d = tmp_path / "fss" / ("L%d" % L)
+    wfile = [f for f in os.listdir(d) if f.startswith("weight_gpu1_")][0]
+    txt = (d / wfile).read_text()
+    (d / "weight_mpi_T050c16_M200_JACK0_DKL1e-4.txt").write_text(txt)
+    lnw_file = np.array([float(line.split()[1]) for line in txt.strip().splitlines()])
+    args = [str(L), "0", "0", str(rng_), str(jacks), str(tm), str(nm), "1.9", "0.1", "--chains=%d" % NW,
+            "--jack-blocks", "--load-chains=%s" % cf]
+    r = subprocess.run([exes[1]] + args, capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stderr
+    name = "observables_gpu1_T050_JACKgpu_THERM%sN_NUP%sN_delta1.9to0.1noreset.txt" % (tm, nm)
+    rows = [list(map(float, ln.split())) for ln in (d / name).read_text().splitlines()]
+    exp = _produce_variants(orc, L, NW, 1, rng_, jacks, tm, nm, 1.9, 0.1, lnw_file, blocks=True,
+                            start_lats=lat)
+    assert len(rows) == rng_
+    for (m, s_, _), row in zip(exp, rows):
+        assert np.all(np.isfinite(row[1:]))
+        np.testing.assert_allclose(row[1:], [m[0], m[1], s_[0], s_[1]], rtol=2e-9, atol=1e-12)
