@@ -101,7 +101,9 @@ __global__ void __launch_bounds__(256) k_sweep_random(const RandomArgs a, uint32
                 r3 = philox<R>(c0, 0xbadbad11u, 2u * iter, kCtrTag, k3);
             }
             const uint32_t idx = __float2uint_rz(__fmul_rn(u01f(pick(r2, sub)), fN));
-            const uint32_t row = idx / L, col = idx - row * L;
+            // idx / L as a high product with ceil(2^32 / L): exact for idx < 2^16
+            // and L <= 128 (the rounding error idx / 2^32 < 1/L)
+            const uint32_t row = __umulhi(idx, a.inv_L), col = idx - row * L;
             uint32_t *pw = lat + (size_t)(row * WPR + (col >> 4)) * cpb;
             const int os = (int)spin_code(*pw, col) - 1;
             int ns = os + ((pick(r3, sub) >> 31) ? -1 : 1);  // u01fixedpt<float>(r3) < 0.5 <=> top bit clear

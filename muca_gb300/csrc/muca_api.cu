@@ -201,6 +201,7 @@ RandomArgs random_args(muca_ctx *c, uint32_t iter, uint32_t seed, uint64_t therm
     a.nup = nup;
     a.logf_tab = c->d_logf_tab;
     a.dyn = nullptr;
+    a.inv_L = (uint32_t)(((1ull << 32) + c->L - 1) / c->L);
     // muca_set_log_bracket widens either bound
     a.log_eps = c->d_logf_tab ? (c->log_eps_table > c->log_eps ? c->log_eps_table : c->log_eps) : c->log_eps;
     return a;

@@ -96,6 +96,8 @@ struct RandomArgs {
     // bound on |__logf(u) - log(u)| over every u01fixedpt<float> value, log
     // being logf_tab's values (when given) or CUDA's logf, with a safety factor
     double log_eps;
+    // ceil(2^32 / L): row = high 32 bits of idx * inv_L for idx < N <= 2^14
+    uint32_t inv_L;
 };
 // Worst case of |__logf(u) - tab[k]| over u = (2k+1) 2^-24, k < 2^23 (exhaustive, on the device).
 cudaError_t measure_table_bracket(const float *tab, float *max_abs_err, cudaStream_t s);

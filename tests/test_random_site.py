@@ -107,3 +107,13 @@ def test_random_site_weight_run_vs_oracle(muca, orc, continuing):
         assert r.width_temp == int(rec[k, 0]), k
         assert r.total_run == int(rec[k, 3]), k
     np.testing.assert_allclose(w, lnw, rtol=1e-12, atol=1e-9)
+
+
+def test_row_from_high_product_is_exact():
+    """The random-site kernel forms row = idx / L as the high 32 bits of
+    idx * ceil(2^32 / L); exact for every site index of every L in 3..128."""
+    for L in range(3, 129):
+        N = L * L
+        inv = ((1 << 32) + L - 1) // L
+        idx = np.arange(N, dtype=np.uint64)
+        assert np.array_equal((idx * np.uint64(inv)) >> np.uint64(32), idx // np.uint64(L)), L
