@@ -232,7 +232,7 @@ def held_out_instances(Ls, Ts, rng, chains):
 def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, held_T=(0.43, 0.53, 0.63, 0.73),
               held_L=(), schedule=4, steps=10000, device=0, reference_criterion=True, agreement_Lmax=48,
               graded=False, ab_schedules=(), save=None, load=None, progress=None, held_sizes=None, nup_max=None,
-              max_iter=None):
+              max_iter=None, starting_sweeps=None):
     """The study: training data from the batched engine (every (L, T) on the
     grid, a seed per instance, DATA_OPTS), the network trained on the
     device, the A/B on the held-out (L, T, Delta) to min/mean >= 0.5 with one
@@ -257,6 +257,8 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
         opts["nup_max"] = nup_max
     if max_iter:
         opts["max_iter"] = max_iter
+    if starting_sweeps:
+        opts["starting_sweeps"] = starting_sweeps
     out = {"run_opts": dict(opts), "data_opts": dict(DATA_OPTS)}
     with m.MLP(device=device, seed=7) as net:
         if load:
@@ -341,6 +343,8 @@ def main(argv=None):
     p.add_argument("--held-sizes", default="", help="run the A/B only on the held-out instances of these sizes")
     p.add_argument("--nup-max", type=int, default=0, help="NUPDATES cap of the A/B (0: RUN_OPTS')")
     p.add_argument("--max-iter", type=int, default=0, help="iteration cap of the A/B (0: RUN_OPTS')")
+    p.add_argument("--starting-sweeps", type=int, default=0,
+                   help="initial NUPDATES of the A/B in sweeps of each instance (0: RUN_OPTS')")
     p.add_argument("--ab-schedules", default="",
                    help="NUPDATES schedules to repeat the A/B with (same network), e.g. 0,4")
     p.add_argument("--no-reference-criterion", action="store_true",
@@ -354,7 +358,8 @@ def main(argv=None):
                     agreement_Lmax=a.agreement_Lmax, graded=a.graded,
                     ab_schedules=[int(v) for v in a.ab_schedules.split(",") if v], save=a.save, load=a.load,
                     progress=a.progress, held_sizes=[int(v) for v in a.held_sizes.split(",") if v],
-                    nup_max=a.nup_max or None, max_iter=a.max_iter or None)
+                    nup_max=a.nup_max or None, max_iter=a.max_iter or None,
+                    starting_sweeps=a.starting_sweeps or None)
     print(json.dumps(out))
     return out
 
