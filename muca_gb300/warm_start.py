@@ -26,13 +26,14 @@ import numpy as np
 
 import muca_gb300 as m
 
-# the weight iteration used for the training data and both arms of the A/B
-# (schedule 4, the CPU program's NUPDATES x1.05 from the first iteration,
-# capped at 2^18 per chain; one schedule for every arm of an A/B)
+# the weight iteration of every arm of the A/B: schedule 4 (the CPU
+# program's NUPDATES x1.05 per iteration) from 16 sweeps of the instance,
+# capped at 2^18 attempts per chain; one schedule for every arm
 RUN_OPTS = dict(starting_M=1, rule=m.UPDATE_TRIVIAL, nup_schedule=4, flat_minmean=1, max_iter=20000,
-                graph_iters=32, starting_sweeps=1, nup_max=1 << 18)
-# the training data: NUPDATES doubling once the width is N (capped at 2^18)
-DATA_OPTS = dict(RUN_OPTS, nup_schedule=1)
+                graph_iters=32, starting_sweeps=16, nup_max=1 << 18)
+# the training data: NUPDATES from one sweep, doubling once the width is N
+# (capped at 2^18)
+DATA_OPTS = dict(RUN_OPTS, nup_schedule=1, starting_sweeps=1)
 
 
 def converge(instances, opts=RUN_OPTS, warm=None, device=0):

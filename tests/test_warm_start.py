@@ -1,12 +1,13 @@
 """The learned warm start end to end on small lattices: converged weights from
 the batched engine train the MLP on the device; on held-out (L, T) the weight
 iteration from the network's prediction reaches the same flat-histogram
-criterion (min/mean >= 0.5) in fewer iterations (at least 1.4x here) and in
-less device time (at least 1.5x) than from the zero weight, with the same
-seeds, options and NUPDATES schedule for every arm (schedule 4, the CPU
-program's x1.05 per iteration, capped at 2^18).  On 12 held-out instances
-at L <= 32 the same settings measured 2.1x fewer iterations and 8.7x less
-device time; this smaller set gains less.  The two non-learned arms (the
+criterion (min/mean >= 0.5) in at least 3x fewer iterations and at least 3x
+less device time than from the zero weight, with the same seeds, options and
+NUPDATES schedule for every arm (schedule 4, the CPU program's x1.05 per
+iteration, from 16 sweeps of the instance, capped at 2^18).  On a GB300 this
+set measured 3.51x fewer iterations and 15.8x less device time; the 12
+held-out instances at L in {16, 24, 32} of the larger study measured 3.73x
+and 4.13x with the same settings.  The two non-learned arms (the
 reference's piecewise-linear form and the full weights, interpolated in T)
 run beside it and converge."""
 import numpy as np
@@ -34,8 +35,8 @@ def test_warm_start_cuts_iterations_and_time(muca):
     assert all(r[k + "_converged"] for r in rows for k in ("zero", "mlp", "pl", "interp"))
     print("warm start: iterations ratio %.2f, device time ratio %.2f, interp %.2f / %.2f" % (
         ab["iters_ratio"], ab["time_ratio"], ab["interp_iters_ratio"], ab["interp_time_ratio"]))
-    assert ab["iters_ratio"] >= 1.4, ab
-    assert ab["time_ratio"] >= 1.5, ab
+    assert ab["iters_ratio"] >= 3.0, ab
+    assert ab["time_ratio"] >= 3.0, ab
     # the surrogate is within a few units of lnW over a range of hundreds
     for r in rows:
         assert r["surrogate_lnw_rms_err"] < 0.05 * r["lnw_range"], r
