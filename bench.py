@@ -179,6 +179,21 @@ def issue_roofline(prof, sweep_s, clk, sms):
             "instructions_source": prof.get("source")}
 
 
+def sweep_floor(local, sweep_s, attempts_per_chain, clk):
+    """The weight sweep taken apart (muca_sweep_floor): SM cycles per attempt
+    of one warp for the whole window and for each of its parts, beside the
+    launch's own cycles per attempt per warp (event time x sampled SM clock /
+    attempts per chain; one warp per SM sub-partition, as in the parts)."""
+    import muca_gb300 as m
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    out = {"unit": "SM cycles per attempt per warp", "geometry": "one block of 4 warps x 32 chains on one SM, "
+           "L=72, lattice, FP32 weights and u32 histogram in shared memory, 4096 windows of 8 attempts per lane"}
+    for part, name in enumerate(m.SWEEP_FLOOR_PARTS):
+        out[name] = m.sweep_floor(part, local)
+    out["kernel"] = sweep_s * mhz * 1e6 / attempts_per_chain
+    return out
+
+
 def cpu_oracle_rate(L, chains, nthreads, min_seconds=12.0, max_reps=200):
     """The reference algorithm on the host: full steps (therm=N, nup=N) of
     `chains` chains with `nthreads` POSIX threads; returns (attempts/ns, sample)."""
@@ -380,6 +395,7 @@ def ours_arm(args, ws, rank, local):
                              "frac": PHILOX_BLOCKS_PER_ATTEMPT * att_rate / philox_peak,
                              "peak_source": "measured (muca_philox_peak on this GPU)"},
             "roofline_issue": issue_roofline(prof, sweep_avg, clk, eng.info.sms),
+            "sweep_floor": sweep_floor(local, sweep_avg, 2 * N, clk),
             "sweep_ms": 1e3 * sweep_avg, "init_ms": init_ms, "gpu_launches": 4 * args.steps,  # per step: the sweep and the three passes of the update
             "clocks": clk, "wall_s_timed_region": t_wall,
         }

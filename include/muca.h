@@ -314,6 +314,19 @@ muca_status muca_jackknife(muca_ctx *ctx, const double *x, uint32_t n, double *a
  * integer-pipe ceiling against which the sweep kernels are reported. */
 muca_status muca_philox_peak(int32_t device, uint32_t rounds, double *blocks_per_s);
 
+/* Measurement (no reference counterpart): the weight-mode windowed sweep
+ * taken apart, timed per warp in SM cycles per attempt, in the sweep's
+ * geometry at 16384 chains (one block of four warps on one SM, L = 72,
+ * lattice, FP32 weights and u32 histogram in shared memory).  part 0: the
+ * whole window (draws of the next window, decode, scan, store, histogram);
+ * 1: draws and decode alone; 2: scan, store and histogram alone on decoded
+ * windows; 3: the bare chain of accept/reject decisions; 4: the draws alone;
+ * 5: one dependent FP32 add per attempt slot (its latency); 6: one dependent
+ * shared-memory load per attempt slot (its latency).  `windows` (even,
+ * 2..2^20) 8-slot windows per lane; the slowest warp is reported.  The
+ * caller's current device is the same after the call as before. */
+muca_status muca_sweep_floor(int32_t device, uint32_t part, uint32_t windows, double *cycles_per_attempt);
+
 /* ---- Batches of independent weight runs (no counterpart in the reference) ----
  * The reference estimates one (L, T) weight per program run.  A batch runs
  * many such estimations of uneven size together on one GPU: every iteration

@@ -37,7 +37,7 @@ EXPORTS = [
     "muca_clear_histogram", "muca_get_histogram", "muca_set_histogram", "muca_histogram_stats", "muca_update_weights",
     "muca_iterate_host",
     "muca_weight_run", "muca_weight_shift", "muca_compute_observables", "muca_jackknife",
-    "muca_philox_peak", "muca_weight_run_stream", "muca_get_reweighting_weights",
+    "muca_philox_peak", "muca_sweep_floor", "muca_weight_run_stream", "muca_get_reweighting_weights",
     "muca_observables_noalloc",
     "muca_batch_create", "muca_batch_destroy", "muca_batch_last_error", "muca_batch_get_info",
     "muca_batch_init_chains", "muca_batch_set_weights", "muca_batch_get_weights", "muca_batch_get_histogram",
@@ -188,6 +188,7 @@ def lib():
     L.muca_compute_observables.argtypes = [vp, C.c_double, C.c_double, C.POINTER(Observables)]
     L.muca_jackknife.argtypes = [vp, f64, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.muca_philox_peak.argtypes = [C.c_int32, C.c_uint32, C.POINTER(C.c_double)]
+    L.muca_sweep_floor.argtypes = [C.c_int32, C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]
     L.muca_observables_noalloc.argtypes = [C.c_int32, vp, vp, C.c_uint32, C.c_double, C.c_double, vp, vp]
     L.muca_batch_create.argtypes = [C.POINTER(BatchParams), C.POINTER(Instance), C.c_uint32, C.POINTER(vp)]
     L.muca_batch_destroy.argtypes = [vp]
@@ -220,6 +221,23 @@ def philox_peak(device: int = 0, rounds: int = 7) -> float:
     """Measured Philox4x32-R blocks per second on this GPU (integer-pipe ceiling)."""
     out = C.c_double()
     st = lib().muca_philox_peak(device, rounds, C.byref(out))
+    if st:
+        raise MucaError(st, lib().muca_last_error(None).decode())
+    return out.value
+
+
+SWEEP_FLOOR_PARTS = ("whole_window", "draws_and_decode", "scan_store_histogram", "decision_chain", "draws",
+                     "fp32_add_latency", "shared_load_latency")
+
+
+def sweep_floor(part: int, device: int = 0, windows: int = 4096) -> float:
+    """SM cycles per attempt of one warp for a part of the weight-mode
+    windowed sweep at L = 72 (muca_sweep_floor): 0 the whole window, 1 draws
+    and decode, 2 scan, store and histogram, 3 the bare decision chain, 4 the
+    draws; 5 and 6 the latency of one dependent FP32 add and of one
+    dependent shared-memory load."""
+    out = C.c_double()
+    st = lib().muca_sweep_floor(device, part, windows, C.byref(out))
     if st:
         raise MucaError(st, lib().muca_last_error(None).decode())
     return out.value

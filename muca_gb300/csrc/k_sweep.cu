@@ -54,7 +54,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_win(const SweepArgs a, uint32_
     uint32_t iter;
     unsigned long long nup;
     if (!launch_params(a, iter, nup)) return;
-    win_sweep_block<MODE, R, LAT_SMEM, true, false, RING>(a, smem, cpb, blockIdx.x, iter, nup);
+    // with the lattice behind the row ring the scan fetches weights three
+    // attempts ahead (measured faster there, slower with the lattice in
+    // shared memory)
+    win_sweep_block<MODE, R, LAT_SMEM, true, false, RING, RING>(a, smem, cpb, blockIdx.x, iter, nup);
 }
 
 // ---------------------------------------------------------------------------
@@ -259,7 +262,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_spec(const SweepArgs a, uint32
     } else {
         const bool store = lane < cpb;
         ChainState st;
-        st.E = cs.active ? a.edel[cs.chain] : (store ? 0 : 2);
+        st.E = cs.active ? a.edel[cs.chain] : (store ? 0 : 3);
         st.EJ = cs.active ? a.ej[cs.chain] : 0;
         st.M = (cs.active && MODE == kModeProduce) ? a.mag[cs.chain] : 0;
         const WT eps = (WT)a.log_eps;

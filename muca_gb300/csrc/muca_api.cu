@@ -981,4 +981,35 @@ muca_status muca_philox_peak(int32_t device, uint32_t rounds, double *blocks_per
     return MUCA_OK;
 }
 
+muca_status muca_sweep_floor(int32_t device, uint32_t part, uint32_t windows, double *cycles_per_attempt)
+{
+    if (!cycles_per_attempt) return fail(nullptr, MUCA_ERR_BAD_ARG, "NULL argument");
+    if (part > 6 || windows < 2 || windows > (1u << 20) || (windows & 1u))
+        return fail(nullptr, MUCA_ERR_BAD_ARG, "part=%u windows=%u", part, windows);
+    int prev = 0;
+    CUDA_TRY(nullptr, cudaGetDevice(&prev));
+    CUDA_TRY(nullptr, cudaSetDevice(device));
+    unsigned long long *cyc = nullptr, *hd = nullptr;
+    uint32_t *sink = nullptr;
+    cudaError_t err = cudaMalloc(&cyc, 4 * sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaMalloc(&hd, sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaMalloc(&sink, 128 * sizeof(uint32_t));
+    unsigned long long h[4] = {0, 0, 0, 0};
+    // one launch to warm up, then the measured one
+    for (int rep = 0; rep < 2 && err == cudaSuccess; ++rep) {
+        err = launch_sweep_floor((int)part, windows, cyc, sink, hd, 0);
+        if (err == cudaSuccess) err = cudaDeviceSynchronize();
+    }
+    if (err == cudaSuccess) err = cudaMemcpy(h, cyc, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(cyc);
+    cudaFree(hd);
+    cudaFree(sink);
+    cudaSetDevice(prev);
+    if (err != cudaSuccess) return fail(nullptr, MUCA_ERR_CUDA, "sweep floor: %s", cudaGetErrorString(err));
+    unsigned long long mx = 0;
+    for (int w = 0; w < 4; ++w) mx = h[w] > mx ? h[w] : mx;
+    *cycles_per_attempt = (double)mx / (8.0 * windows);
+    return MUCA_OK;
+}
+
 }  // extern "C"

@@ -276,5 +276,8 @@ cudaError_t launch_mlp_step(float *P, float *G, float *m, float *v, const float 
 // Philox throughput microbenchmark (k_bench.cu): grid blocks of 256 threads,
 // each generating blocks_per_thread Philox4x32-R blocks.
 cudaError_t launch_philox_peak(int rounds, uint32_t grid, uint32_t blocks_per_thread, uint32_t *out, cudaStream_t s);
+// the weight-mode windowed sweep taken apart (part 0..3), cycles per warp of `windows` 8-site windows
+cudaError_t launch_sweep_floor(int part, uint32_t windows, unsigned long long *cycles, uint32_t *sink,
+                               unsigned long long *hist_dummy, cudaStream_t s);
 
 }  // namespace muca

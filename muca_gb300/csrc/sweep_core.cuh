@@ -218,10 +218,15 @@ __device__ __forceinline__ void decode_window(uint32_t *__restrict__ lat, uint32
 
 // The accept/reject scan of a decoded window, its lattice write and its
 // histogram entries.  ONEBAND (weight mode): decide each attempt with the
-// one-band test of the production scan instead of the two tests.  `store` is false for padding lanes: they read another
-// lane's spins, never accept (so their E stays at 2 and every weight index
-// E + dDel_t + dDel_t+1 stays in [0, 4]) and never write.
-template <int MODE, int SLOTS, bool HS = true, bool ONEBAND = false>
+// one-band test of the production scan instead of the two tests.  AHEAD2
+// (weight mode): fetch each attempt's weight three attempts ahead, for the
+// four outcomes of the two decisions between, instead of one attempt ahead
+// for two outcomes.  Both forms decide every attempt identically; which is
+// faster depends on the kernel around the scan (measured per kernel).
+// `store` is false for padding lanes: they read another lane's spins, never
+// accept (so their E stays at 3 and every weight index E + dDel_t + dDel_t+1
+// + dDel_t+2 stays in [0, 6]) and never write.
+template <int MODE, int SLOTS, bool HS = true, bool ONEBAND = false, bool AHEAD2 = false>
 __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, bool store, bool checked,
                                             const typename WeightType<MODE>::T *__restrict__ wS,
                                             uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
@@ -306,15 +311,77 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
     const ChainState s0 = st;
     const WT wE0 = wS[st.E];
     WT wE = wE0;
+    uint32_t accm = 0;
+    bool near = false;
+    int Es[SLOTS], Ms[SLOTS];
+    if constexpr (AHEAD2) {
+        // P[u][2a + b]: the weight at attempt u's proposed E_Delta when the
+        // attempts u-2 and u-1 decide a and b, loaded after attempt u-3
+        WT P[SLOTS][4];
+        bool av[SLOTS];
+        P[0][0] = wS[st.E + d.dDel[0]];
+        if (SLOTS > 1) {
+            P[1][0] = wS[st.E + d.dDel[1]];
+            P[1][1] = wS[st.E + d.dDel[0] + d.dDel[1]];
+        }
+        if (SLOTS > 2) {
+            P[2][0] = wS[st.E + d.dDel[2]];
+            P[2][1] = wS[st.E + d.dDel[1] + d.dDel[2]];
+            P[2][2] = wS[st.E + d.dDel[0] + d.dDel[2]];
+            P[2][3] = wS[st.E + d.dDel[0] + d.dDel[1] + d.dDel[2]];
+        }
+#pragma unroll
+        for (int t = 0; t < SLOTS; ++t) {
+            WT A;
+            if (t == 0) {
+                A = P[0][0];
+            } else if (t == 1) {
+                A = av[0] ? P[1][1] : P[1][0];
+            } else {
+                const WT q0 = av[t - 2] ? P[t][2] : P[t][0];
+                const WT q1 = av[t - 2] ? P[t][3] : P[t][1];
+                A = av[t - 1] ? q1 : q0;
+            }
+            WT diff;
+            if (MODE == kModeWeight)
+                diff = __fsub_rn(__fadd_rn((float)d.f2[t], (float)A), (float)wE);
+            else
+                diff = __dsub_rn(__dadd_rn((double)d.f2[t], (double)A), (double)wE);
+            const WT l = (WT)d.lf[t];
+            bool acc;
+            if (ONEBAND) {
+                const WT g = l - diff;
+                acc = store && (g < (WT)0);
+                near |= fabs(g) <= eps;
+            } else {
+                acc = store && ((diff >= (WT)0) || (l < diff));
+                near |= (diff < (WT)0) && (fabs(l - diff) <= eps);
+            }
+            av[t] = acc;
+            if (acc) {
+                st.E += d.dDel[t];
+                st.EJ += d.dE[t];
+                st.M += d.dM[t];
+                wE = A;
+                accm |= 0xFu << (4 * t);
+            }
+            Es[t] = st.E;
+            Ms[t] = st.M;
+            if (t + 3 < SLOTS) {
+                const int e = st.E + d.dDel[t + 3];
+                P[t + 3][0] = wS[e];
+                P[t + 3][1] = wS[e + d.dDel[t + 2]];
+                P[t + 3][2] = wS[e + d.dDel[t + 1]];
+                P[t + 3][3] = wS[e + d.dDel[t + 1] + d.dDel[t + 2]];
+            }
+        }
+    } else {
     WT A = wS[st.E + d.dDel[0]];
     WT c0 = A, c1 = A;
     if (SLOTS > 1) {
         c0 = wS[st.E + d.dDel[1]];
         c1 = wS[st.E + d.dDel[0] + d.dDel[1]];
     }
-    uint32_t accm = 0;
-    bool near = false;
-    int Es[SLOTS], Ms[SLOTS];
 #pragma unroll
     for (int t = 0; t < SLOTS; ++t) {
         WT diff;
@@ -353,6 +420,7 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
             }
         }
     }
+    }
     if (__any_sync(0xffffffffu, near)) {
         st = s0;
         wE = wE0;
@@ -385,7 +453,7 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
 }
 
 // One full window: decode, then scan.
-template <int MODE, int SLOTS, int HALF, bool HS = true, bool BT = false>
+template <int MODE, int SLOTS, int HALF, bool HS = true, bool BT = false, bool AHEAD2 = false>
 __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t cpb, uint32_t L, uint32_t WPR,
                                             uint32_t row, uint32_t q, bool rec, bool store, bool checked,
                                             const typename WeightType<MODE>::T *__restrict__ wS,
@@ -398,9 +466,10 @@ __device__ __forceinline__ void window_core(uint32_t *__restrict__ lat, uint32_t
     WinDec<MODE> d;
     decode_window<MODE, SLOTS, BT>(lat, cpb, L, WPR, row, q, HALF < 0 ? hrt : (uint32_t)HALF, r1, r3, btab, d,
                                    rmask);
-    // the batch kernel (the one user of the beta table) decides weight-mode
-    // attempts with the one-band test
-    scan_window<MODE, SLOTS, HS, BT>(d, rec, store, checked, wS, histS, histG, st, eps, wG, tol);
+    // the batch kernel (the one user of the beta table) and the scan with
+    // weights fetched three attempts ahead decide weight-mode attempts with
+    // the one-band test
+    scan_window<MODE, SLOTS, HS, BT || AHEAD2, AHEAD2>(d, rec, store, checked, wS, histS, histG, st, eps, wG, tol);
 }
 
 // The first `len` (< window size) attempts of a window, one at a time as
@@ -694,7 +763,7 @@ __device__ __forceinline__ bool launch_params(const SweepArgs &a, uint32_t &iter
 // RING (with LAT_SMEM false): the lattice stays in global memory and each
 // lane keeps a four-row ring of its chain in shared memory (RowRing), at the
 // offset where the whole lattice would go.
-template <int MODE, int R, bool LAT_SMEM, bool HS = true, bool BT = false, bool RING = false>
+template <int MODE, int R, bool LAT_SMEM, bool HS = true, bool BT = false, bool RING = false, bool AHEAD2 = false>
 __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned char *smem, uint32_t cpb, uint32_t blk,
                                                 uint32_t iter, unsigned long long nup,
                                                 const float *__restrict__ btab = nullptr)
@@ -722,7 +791,7 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
     cs.init(a, cpb, lane, blk);
     const bool store = lane < cpb;
     ChainState st;
-    st.E = cs.active ? a.edel[cs.chain] : (store ? 0 : 2);
+    st.E = cs.active ? a.edel[cs.chain] : (store ? 0 : 3);
     st.EJ = cs.active ? a.ej[cs.chain] : 0;
     st.M = (cs.active && MODE == kModeProduce) ? a.mag[cs.chain] : 0;
     const WT eps = (WT)a.log_eps;
@@ -768,7 +837,7 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
                 r3[t] = n3[t];
             }
             advance(2);  // independent of the window below: overlaps its scan
-            window_core<MODE, 8, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
+            window_core<MODE, 8, -1, HS, BT, AHEAD2>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
                                              r3, eps, btab, half, wG, tol, rmask);
         } else {
             uint32_t r1[4], r3[4];
@@ -778,7 +847,7 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
                 r3[t] = n3[t];
             }
             advance(1);
-            window_core<MODE, 4, -1, HS, BT>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
+            window_core<MODE, 4, -1, HS, BT, AHEAD2>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
                                              r3, eps, btab, half, wG, tol, rmask);
         }
         return true;

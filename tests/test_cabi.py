@@ -57,6 +57,12 @@ def test_null_arguments(libmuca):
     assert libmuca.muca_set_log_bracket(None, 1e30) == 1
     assert libmuca.muca_set_wait_limit(None, 1000) == 1
     assert libmuca.muca_set_test_hooks(None, 0) == 1
+    # measurement calls check their arguments before any device work
+    out = C.c_double()
+    assert libmuca.muca_sweep_floor(0, 0, 4096, None) == 1
+    assert libmuca.muca_sweep_floor(0, 7, 4096, C.byref(out)) == 1
+    assert libmuca.muca_sweep_floor(0, 0, 4097, C.byref(out)) == 1
+    assert libmuca.muca_sweep_floor(0, 0, 0, C.byref(out)) == 1
 
 
 def test_no_gpu_fails_loudly(libmuca):
