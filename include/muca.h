@@ -202,11 +202,16 @@ muca_status muca_set_log_bracket(muca_ctx *ctx, double bracket);
  * chains' state after such a launch is not valid).  The bound is per wait, so
  * a long launch that keeps making progress never times out. */
 muca_status muca_set_wait_limit(muca_ctx *ctx, uint64_t cycles);
-/* Test hooks, for tests of the timeout path only (0 in normal use).
+/* Test hooks, for tests only (0 in normal use).
  * MUCA_HOOK_SILENT_PRODUCER: the producer warps of the warp-specialised sweep
  * never signal a filled ring slot, so the consumers' bounded waits run out.
- * Nothing faults and every wait stays bounded. */
+ * Nothing faults and every wait stays bounded.
+ * MUCA_HOOK_FLUSH_ROWS: the windowed sweep flushes its shared u32 histogram
+ * bins into the device histogram before every row it records, the path a
+ * launch takes when its bins could otherwise reach 2^32 (results are the
+ * same bit for bit). */
 #define MUCA_HOOK_SILENT_PRODUCER 1u
+#define MUCA_HOOK_FLUSH_ROWS 2u
 muca_status muca_set_test_hooks(muca_ctx *ctx, uint32_t hooks);
 
 /* Chains.  Replaces the host lattice init (muca_delta_multigpu.cu:340-354,

@@ -26,6 +26,7 @@ ALGO_SWEEP, ALGO_RANDOM_SITE = 0, 1
 UPDATE_TRIVIAL, UPDATE_TRIVIAL_CPU, UPDATE_RECURSION = 0, 1, 2
 KERNEL_AUTO, KERNEL_GENERIC, KERNEL_WINDOWED, KERNEL_SPECIALIZED = 0, 1, 2, 3
 HOOK_SILENT_PRODUCER = 1
+HOOK_FLUSH_ROWS = 2
 STATUS = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "TIMEOUT", 4: "NOT_CONVERGED", 5: "IO", 6: "STATE"}
 
 # Every symbol include/muca.h declares (the C-ABI surface).
@@ -350,7 +351,7 @@ class Engine:
         self._ck(self._lib.muca_set_wait_limit(self._h, int(cycles)))
 
     def set_test_hooks(self, hooks):
-        """Test hooks of the timeout path (HOOK_SILENT_PRODUCER); 0 = none."""
+        """Test hooks (HOOK_SILENT_PRODUCER, HOOK_FLUSH_ROWS); 0 = none."""
         self._ck(self._lib.muca_set_test_hooks(self._h, int(hooks)))
 
     def clear_histogram(self):

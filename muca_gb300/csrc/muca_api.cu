@@ -427,8 +427,10 @@ muca_status muca_set_wait_limit(muca_ctx *c, uint64_t cycles)
 muca_status muca_set_test_hooks(muca_ctx *c, uint32_t hooks)
 {
     if (!c) return fail(nullptr, MUCA_ERR_BAD_ARG, "ctx is NULL");
-    if (hooks & ~(uint32_t)MUCA_HOOK_SILENT_PRODUCER) return fail(c, MUCA_ERR_BAD_ARG, "unknown hook bits 0x%x", hooks);
-    static_assert(MUCA_HOOK_SILENT_PRODUCER == kHookSilentProducer, "hook bits");
+    if (hooks & ~(uint32_t)(MUCA_HOOK_SILENT_PRODUCER | MUCA_HOOK_FLUSH_ROWS))
+        return fail(c, MUCA_ERR_BAD_ARG, "unknown hook bits 0x%x", hooks);
+    static_assert(MUCA_HOOK_SILENT_PRODUCER == kHookSilentProducer && MUCA_HOOK_FLUSH_ROWS == kHookFlushRows,
+                  "hook bits");
     c->hooks = hooks;
     return MUCA_OK;
 }

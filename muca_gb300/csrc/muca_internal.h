@@ -46,6 +46,9 @@ constexpr long long kWaitCyclesDefault = 1ll << 34;
 // launch ends with the error word set (a test of the timeout path; it faults
 // nothing and every wait stays bounded)
 constexpr uint32_t kHookSilentProducer = 1u;
+// kHookFlushRows: the windowed sweep flushes its shared u32 bins before every
+// recorded row, as a launch that could fill a bin does
+constexpr uint32_t kHookFlushRows = 2u;
 
 enum SweepMode { kModeWeight = 0, kModeProduce = 1 };
 

@@ -79,7 +79,8 @@ __device__ __forceinline__ void record(uint32_t *histS, unsigned long long *hist
 // Histogram entries of one window.  Weight mode with the shared u32
 // histogram: one shared atomic per attempt; `checked` (uniform: the launch
 // can put 2^32 entries into one block's bins) drains a u32 shared bin into
-// the u64 device histogram once it holds 2^31.  Device (u64) histograms:
+// the u64 device histogram once it holds 2^31 (the warp-specialised sweep;
+// the windowed sweep flushes all bins between rows instead, flush_hist).  Device (u64) histograms:
 // the entries are merged into runs of equal bins per lane first (E_Delta
 // moves by at most one per attempt, so a window's entries cluster), which
 // saves global atomics; HS = false (weight mode) sends the runs straight to
@@ -690,6 +691,22 @@ __host__ __device__ inline size_t ring_bytes(uint32_t L, uint32_t cpb)
     return (size_t)4 * ((L + 15) / 16) * cpb * 4;
 }
 
+// Moves the shared u32 bins into the u64 device histogram and clears them;
+// every thread of the block calls it (it holds two block barriers).
+template <int MODE>
+__device__ __forceinline__ void flush_hist(uint32_t *histS, unsigned long long *histG, uint32_t N)
+{
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b <= N; b += blockDim.x) {
+        const uint32_t v = histS[b];
+        if (v) {
+            atomicAdd(&histG[b], (unsigned long long)v);
+            histS[b] = 0;
+        }
+    }
+    __syncthreads();
+}
+
 template <int MODE>
 __device__ __forceinline__ void drain_hist(uint32_t *histS, unsigned long long *histG, uint32_t N)
 {
@@ -795,8 +812,6 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
     st.EJ = cs.active ? a.ej[cs.chain] : 0;
     st.M = (cs.active && MODE == kModeProduce) ? a.mag[cs.chain] : 0;
     const WT eps = (WT)a.log_eps;
-    // u32 shared bins can overflow only if the launch can record 2^32 entries in one block
-    const bool checked = (unsigned long long)cpb * nup >= 0xFFFFFFFFull;
     const uint32_t L = a.L, WPR = a.WPR;
     // draws of the next two groups (counters cc - 1, cc), the two streams apart
     uint32_t n1[8], n3[8];
@@ -818,40 +833,71 @@ __device__ __forceinline__ void win_sweep_block(const SweepArgs &a, unsigned cha
             cc += 1;
         }
     };
-    for_each_window(L, WPR, a.therm, nup, [&](uint32_t row, uint32_t q, uint32_t half, uint32_t cnt, uint32_t len,
-                                              bool rec_phase) {
-        const bool rec = rec_phase && cs.active;
-        if (RING && q == 0) ring.row_start(row, L, cpb, WPR, store);
-        if (len < cnt) {
-            uint32_t p[8];
-#pragma unroll
-            for (int t = 0; t < 8; ++t) p[t] = pack_draw(n1[t], n3[t]);
-            partial_core<MODE, HS, BT>(lat, cpb, L, WPR, row, q, half, len, rec, store, wP, histS, a.hist, st, p, btab,
-                                       rmask);
-            advance((len + 3u) >> 2);
-        } else if (cnt == 8) {
-            uint32_t r1[8], r3[8];
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                r1[t] = n1[t];
-                r3[t] = n3[t];
+    // The reference's sweep order (for_each_window's): whole row-halves as a
+    // loop of full windows, W8 words of 8 same-parity sites and, with
+    // L % 16 == 8, one word of 4; a phase's last, partial row-half (only when
+    // therm or nup is not a multiple of L/2) step by step.
+    const uint32_t W8 = L >> 4, per_row = L >> 1;
+    const bool tail4 = (L & 15u) != 0;
+    // recorded attempts per lane since the shared u32 bins were last flushed:
+    // no bin can reach 2^32 while cpb * since stays below it
+    unsigned long long since = 0;
+    for (int phase = 0; phase < 2; ++phase) {
+        unsigned long long n = phase ? nup : a.therm;
+        const bool rec = phase == 1 && cs.active;
+        uint32_t row = 0, half = 0;
+        while (n >= per_row) {
+            if (RING) ring.row_start(row, L, cpb, WPR, store);
+            if (HS && MODE == kModeWeight && phase == 1) {
+                if ((since + per_row) * cpb > 0xFFFFFFFFull || (a.hooks & kHookFlushRows)) {  // uniform
+                    flush_hist<MODE>(histS, a.hist, a.N);
+                    since = 0;
+                }
+                since += per_row;
             }
-            advance(2);  // independent of the window below: overlaps its scan
-            window_core<MODE, 8, -1, HS, BT, AHEAD2>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
-                                             r3, eps, btab, half, wG, tol, rmask);
-        } else {
-            uint32_t r1[4], r3[4];
+            for (uint32_t q = 0; q < W8; ++q) {
+                uint32_t r1[8], r3[8];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                r1[t] = n1[t];
-                r3[t] = n3[t];
+                for (int t = 0; t < 8; ++t) {
+                    r1[t] = n1[t];
+                    r3[t] = n3[t];
+                }
+                advance(2);  // independent of the window below: overlaps its scan
+                window_core<MODE, 8, -1, HS, BT, AHEAD2>(lat, cpb, L, WPR, row, q, rec, store, false, wS, histS,
+                                                         a.hist, st, r1, r3, eps, btab, half, wG, tol, rmask);
             }
-            advance(1);
-            window_core<MODE, 4, -1, HS, BT, AHEAD2>(lat, cpb, L, WPR, row, q, rec, store, checked, wS, histS, a.hist, st, r1,
-                                             r3, eps, btab, half, wG, tol, rmask);
+            if (tail4) {
+                uint32_t r1[4], r3[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    r1[t] = n1[t];
+                    r3[t] = n3[t];
+                }
+                advance(1);
+                window_core<MODE, 4, -1, HS, BT, AHEAD2>(lat, cpb, L, WPR, row, W8, rec, store, false, wS, histS,
+                                                         a.hist, st, r1, r3, eps, btab, half, wG, tol, rmask);
+            }
+            n -= per_row;
+            if (++row == L) {
+                row = 0;
+                half ^= 1u;
+            }
         }
-        return true;
-    });
+        if (n) {
+            if (RING) ring.row_start(row, L, cpb, WPR, store);
+            for (uint32_t q = 0; n; ++q) {
+                const uint32_t cnt = (min(16u * q + 16u, L) - 16u * q) >> 1;
+                const uint32_t len = n < cnt ? (uint32_t)n : cnt;
+                uint32_t p[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) p[t] = pack_draw(n1[t], n3[t]);
+                partial_core<MODE, HS, BT>(lat, cpb, L, WPR, row, q, half, len, rec, store, wP, histS, a.hist, st, p,
+                                           btab, rmask);
+                advance((len + 3u) >> 2);
+                n -= len;
+            }
+        }
+    }
     if (LAT_SMEM && store) {
         const uint32_t words = L * WPR;
         for (uint32_t w = 0; w < words; ++w) gl[(size_t)w * cpb] = lat[(size_t)w * cpb];

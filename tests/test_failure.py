@@ -82,4 +82,4 @@ def test_wait_limit_and_hooks_are_checked(muca):
         with pytest.raises(muca.MucaError):
             e.set_wait_limit(1 << 41)
         with pytest.raises(muca.MucaError):
-            e.set_test_hooks(2)
+            e.set_test_hooks(4)
