@@ -539,24 +539,33 @@ def config2_metric(local, steps=10):
 
 
 def warm_start_metric(local):
-    """The learned warm start (the L=72 configuration's second metric with the
-    network's initial weight, on the batched configuration's instances):
-    converged weights of every (L, T) on a grid (L in {16..128}, 256 chains
-    each) train the MLP on the device; 32 held-out (L, T, Delta) then run the
-    weight iteration from the zero weight, from the network's weight and from
-    two non-learned starts, one NUPDATES schedule for every arm, to
-    min/mean >= 0.5 (iterations, device and wall time) and to the
-    reference's criterion width == N and D_KL < 1e-4 (agreement of the final
-    weights with the zero arm's, beside the zero weight on other seeds).
-    Minutes of GPU time: not part of the default line."""
+    """The learned warm start on the batched configuration's instances:
+    converged weights of every (L, T) with L in {16, 24, 32} and T on a grid
+    of 0.40..0.80 in steps of 0.05 (1024 chains each) train the MLP on the
+    device. Then 12 held-out (L, T, Delta) (T in {0.43, 0.53, 0.63, 0.73})
+    run the weight iteration from four starts: the zero weight, the
+    network's weight, and two non-learned starts. Every arm uses one
+    NUPDATES schedule (x1.05 per iteration from 16 sweeps, capped at 2^18)
+    and runs to min/mean >= 0.5; the study reports iterations, device time
+    and wall time. The held-out instances at L = 16 (16384 chains each) then
+    run to width == N and D_KL < 1e-5, for the agreement of the final
+    weights with the zero arm's, beside the zero weight on other seeds. The
+    reference's D_KL < 1e-4 resolves lnW only to a few 1e-2. Minutes of GPU
+    time: not part of the default line."""
     from muca_gb300 import warm_start as ws
-    out = ws.run_study(device=local)
+    out = ws.run_study(Ls=(16, 24, 32), chains=1024, t_step=0.05, held_sizes=(16, 24, 32), device=local,
+                       agreement_Lmax=16, agreement_chains=16384, agreement_nup_max=1 << 21,
+                       agreement_d_kl=1e-5, agreement_max_iter=1000, agreement_arms=("mlp",))
     ab = out["ab"]
+    ag = out.get("agreement_reference_criterion", {})
     out["summary"] = {
         "iters_ratio_mlp_vs_zero": ab["mlp_iters_ratio"], "device_time_ratio_mlp_vs_zero": ab["mlp_time_ratio"],
         "iters_ratio_interp_vs_zero": ab["interp_iters_ratio"],
         "device_time_ratio_interp_vs_zero": ab["interp_time_ratio"],
-        "iters_ratio_pl_vs_zero": ab["pl_iters_ratio"], "device_time_ratio_pl_vs_zero": ab["pl_time_ratio"]}
+        "iters_ratio_pl_vs_zero": ab["pl_iters_ratio"], "device_time_ratio_pl_vs_zero": ab["pl_time_ratio"],
+        "ab_wall_s": ab.get("wall_s"),
+        "final_lnw_rms_mlp_vs_zero_max": ag.get("mlp", {}).get("final_rms_vs_zero_max"),
+        "final_lnw_rms_reseeded_zero_vs_zero_max": ag.get("zero_reseeded", {}).get("final_rms_vs_zero_max")}
     return out
 
 

@@ -194,13 +194,14 @@ def final_agreement(arm_w, zero_w):
     return {"rms": rms, "max": float(np.max(np.abs(f))), "rms_rel_range": rms / rng_ if rng_ > 0 else None}
 
 
-def agreement_under(net, held, sources, opts, device=0):
+def agreement_under(net, held, sources, opts, device=0, arms=("mlp", "interp", "pl")):
     """The arms run to `opts`' stop criterion; each arm's converged weights
     against the zero arm's, beside the statistical floor (the zero weight on
     other seeds against the zero weight)."""
-    arms = {"mlp": [net.log_weights(L, T, D) for L, _, T, D, _ in held],
-            "interp": [interpolated_weight(L, T, sources) for L, _, T, _, _ in held],
-            "pl": [interpolated_weight(L, T, sources, PL_KNOTS) for L, _, T, _, _ in held]}
+    starts = {"mlp": lambda: [net.log_weights(L, T, D) for L, _, T, D, _ in held],
+              "interp": lambda: [interpolated_weight(L, T, sources) for L, _, T, _, _ in held],
+              "pl": lambda: [interpolated_weight(L, T, sources, PL_KNOTS) for L, _, T, _, _ in held]}
+    arms = {k: starts[k]() for k in arms}
     rz, sz, wz = converge(held, opts, None, device)
     out = {"zero": {"iters_total": sum(r.iterations for r in rz), "device_s": sz,
                     "converged": sum(bool(r.converged) for r in rz)}}
@@ -233,7 +234,8 @@ def held_out_instances(Ls, Ts, rng, chains):
 def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, held_T=(0.43, 0.53, 0.63, 0.73),
               held_L=(), schedule=4, steps=10000, device=0, reference_criterion=True, agreement_Lmax=48,
               graded=False, ab_schedules=(), save=None, load=None, progress=None, held_sizes=None, nup_max=None,
-              max_iter=None, starting_sweeps=None):
+              max_iter=None, starting_sweeps=None, agreement_nup_max=1 << 18, agreement_max_iter=40000,
+              agreement_arms=("mlp", "interp", "pl"), agreement_d_kl=1e-4, agreement_chains=None):
     """The study: training data from the batched engine (every (L, T) on the
     grid, a seed per instance, DATA_OPTS), the network trained on the
     device, the A/B on the held-out (L, T, Delta) to min/mean >= 0.5 with one
@@ -245,7 +247,11 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
     an .npz; `load` reads them back instead of generating and training.
     `progress`: a JSON file rewritten with the results so far after every
     stage.  held_sizes: run the A/B only on the held-out instances of these
-    sizes; nup_max / max_iter: the A/B's NUPDATES cap and iteration cap."""
+    sizes; nup_max / max_iter: the A/B's NUPDATES cap and iteration cap;
+    agreement_nup_max / agreement_max_iter / agreement_arms / agreement_d_kl:
+    the NUPDATES cap, iteration cap, warm starts and D_KL bound (1e-4 is the
+    reference's) of the runs to the reference criterion; agreement_chains:
+    their chains per instance (None: `chains`)."""
     t_all = time.time()
 
     def dump(o):
@@ -307,10 +313,11 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
         out["ab"] = ab
         dump(out)
         if reference_criterion:
-            sub = [h for h in held if h[0] <= agreement_Lmax]
-            ro = dict(opts, flat_minmean=0, max_iter=40000, nup_max=1 << 18)
+            sub = [(L, agreement_chains or nc, T, D, seed) for L, nc, T, D, seed in held if L <= agreement_Lmax]
+            ro = dict(opts, flat_minmean=0, max_iter=agreement_max_iter, nup_max=agreement_nup_max,
+                      d_kl_max=agreement_d_kl)
             t0 = time.time()
-            ag = agreement_under(net, sub, sources, ro, device)
+            ag = agreement_under(net, sub, sources, ro, device, agreement_arms)
             ag["wall_s"] = time.time() - t0
             ag["instances"] = [(L, T) for L, _, T, _, _ in sub]
             ag["run_opts"] = ro
@@ -350,6 +357,16 @@ def main(argv=None):
                    help="NUPDATES schedules to repeat the A/B with (same network), e.g. 0,4")
     p.add_argument("--no-reference-criterion", action="store_true",
                    help="skip the runs to width == N and D_KL < 1e-4")
+    p.add_argument("--agreement-nup-max", type=int, default=1 << 18,
+                   help="NUPDATES cap of the runs to the reference criterion")
+    p.add_argument("--agreement-max-iter", type=int, default=40000,
+                   help="iteration cap of the runs to the reference criterion")
+    p.add_argument("--agreement-d-kl", type=float, default=1e-4,
+                   help="D_KL bound of the runs to the reference criterion (the reference's: 1e-4)")
+    p.add_argument("--agreement-chains", type=int, default=0,
+                   help="chains per instance of the runs to the reference criterion (0: --chains)")
+    p.add_argument("--agreement-arms", default="mlp,interp,pl",
+                   help="warm starts run to the reference criterion beside the zero weight and its reseeded floor")
     p.add_argument("--device", type=int, default=0)
     a = p.parse_args(argv)
     out = run_study(Ls=[int(v) for v in a.L.split(",")], chains=a.chains, t_step=a.t_step,
@@ -360,7 +377,10 @@ def main(argv=None):
                     ab_schedules=[int(v) for v in a.ab_schedules.split(",") if v], save=a.save, load=a.load,
                     progress=a.progress, held_sizes=[int(v) for v in a.held_sizes.split(",") if v],
                     nup_max=a.nup_max or None, max_iter=a.max_iter or None,
-                    starting_sweeps=a.starting_sweeps or None)
+                    starting_sweeps=a.starting_sweeps or None, agreement_nup_max=a.agreement_nup_max,
+                    agreement_max_iter=a.agreement_max_iter,
+                    agreement_arms=[v for v in a.agreement_arms.split(",") if v], agreement_d_kl=a.agreement_d_kl,
+                    agreement_chains=a.agreement_chains or None)
     print(json.dumps(out))
     return out
 
