@@ -50,8 +50,9 @@ def _run_produce(muca, L, nch, kernel, lnw, therm, nup, it=5):
     return used, (lat0, ej0, ed0, mg0), (lat1, ej1, ed1, mg1), h
 
 
-# (L, chains, kernel): 0 = the planner's choice (the warp-specialised kernel
-# for production with a global lattice), 1 generic, 2 windowed, 3 specialised;
+# (L, chains, kernel): 0 = the planner's choice (the windowed kernel behind
+# the row ring for production with a global lattice), 1 generic, 2 windowed,
+# 3 specialised;
 # 100 chains leave padding lanes in the last warp
 PRODUCE_CASES = [(128, 128, 0), (128, 64, 1), (128, 64, 2), (128, 100, 3)]
 
@@ -65,7 +66,7 @@ def test_produce_global_lattice_vs_oracle(muca, orc, L, nch, kernel, weights):
     therm, nup = N, 3000 + 7
     used, (lat0, ej0, ed0, mg0), (lat1, ej1, ed1, mg1), h = _run_produce(muca, L, nch, kernel, lnw, therm, nup)
     if kernel == 0:
-        assert used == 3, "the planner's production kernel with a global lattice is the specialised one"
+        assert used == 2, "the planner's production kernel with a global lattice is the windowed one"
     oej, oed, omg = _i32(ej0), _i32(ed0), _i32(mg0)
     olat, oh = orc.produce_sweep(L, lat0.copy(), oej, oed, omg, lnw, 5, SEED, therm, nup, nthreads=8)
     np.testing.assert_array_equal(lat1, olat)
