@@ -226,6 +226,12 @@ def agreement_under(net, held, sources, opts, device=0, arms=("mlp", "interp", "
     return out
 
 
+def agreement_instances(held, Lmax, chains=None):
+    """The held-out instances run to the reference criterion: those with
+    L <= Lmax, with `chains` chains each (None: their own count)."""
+    return [(L, chains or nc, T, D, seed) for L, nc, T, D, seed in held if L <= Lmax]
+
+
 def held_out_instances(Ls, Ts, rng, chains):
     return [(L, chains, float(T), float(rng.uniform(1.5, 1.99)), 5000 + k)
             for k, (L, T) in enumerate([(L, float(T)) for L in Ls for T in Ts])]
@@ -313,7 +319,7 @@ def run_study(Ls=(16, 24, 32, 48, 64, 72, 96, 128), chains=256, t_step=0.025, he
         out["ab"] = ab
         dump(out)
         if reference_criterion:
-            sub = [(L, agreement_chains or nc, T, D, seed) for L, nc, T, D, seed in held if L <= agreement_Lmax]
+            sub = agreement_instances(held, agreement_Lmax, agreement_chains)
             ro = dict(opts, flat_minmean=0, max_iter=agreement_max_iter, nup_max=agreement_nup_max,
                       d_kl_max=agreement_d_kl)
             t0 = time.time()

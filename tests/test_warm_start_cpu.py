@@ -73,3 +73,57 @@ def test_interp_input_checks():
         ws.interpolated_weight(7, 0.5, [])
     with pytest.raises(ValueError):
         ws.interpolated_weight(6, 0.5, [(6, 0.5, np.zeros(10))])
+
+
+def test_final_agreement_ignores_the_additive_constant():
+    rng = np.random.default_rng(0)
+    w = np.cumsum(rng.normal(0, 1, 101))
+    a = ws.final_agreement(w + 3.25, w)
+    assert a["rms"] < 1e-12 and a["max"] < 1e-12
+    d = np.zeros(101)
+    d[50] = 0.101
+    a = ws.final_agreement(w + d, w)
+    f = d - d.mean()
+    assert abs(a["rms"] - np.sqrt(np.mean(f * f))) < 1e-15
+    assert abs(a["max"] - abs(f).max()) < 1e-15
+    assert abs(a["rms_rel_range"] - a["rms"] / (w.max() - w.min())) < 1e-15
+
+
+def test_agreement_instances_take_their_own_chain_count():
+    held = [(16, 1024, 0.43, 1.7, 5000), (24, 1024, 0.53, 1.8, 5001), (16, 1024, 0.63, 1.9, 5002)]
+    assert ws.agreement_instances(held, 16) == [held[0], held[2]]
+    assert ws.agreement_instances(held, 16, 16384) == [(16, 16384, 0.43, 1.7, 5000), (16, 16384, 0.63, 1.9, 5002)]
+    assert ws.agreement_instances(held, 8) == []
+
+
+def test_agreement_under_runs_the_floor_on_other_seeds(monkeypatch):
+    """The zero arm, the requested warm starts and the zero weight on seeds
+    + 7919 (the statistical floor), each compared with the zero arm."""
+    calls = []
+
+    class R:
+        def __init__(self, it):
+            self.iterations, self.converged = it, 1
+
+    def fake_converge(inst, opts, warm=None, device=0):
+        calls.append(([i[4] for i in inst], None if warm is None else [float(w[0]) for w in warm]))
+        off = 0.0 if warm is None else 0.01
+        off += 0.005 if inst[0][4] > 6000 else 0.0
+        return [R(10) for _ in inst], 0.5, [np.linspace(0, 1, 17) + off * np.linspace(-1, 1, 17) for _ in inst]
+
+    class Net:
+        def log_weights(self, L, T, D):
+            return np.full(L * L + 1, 2.0)
+
+    monkeypatch.setattr(ws, "converge", fake_converge)
+    held = [(4, 8, 0.5, 1.9, 100), (4, 8, 0.6, 1.9, 101)]
+    out = ws.agreement_under(Net(), held, [], {"flat_minmean": 0}, arms=("mlp",))
+    assert set(out) == {"zero", "mlp", "zero_reseeded"}
+    seeds = [c[0] for c in calls]
+    assert seeds == [[100, 101], [100 + 7919, 101 + 7919], [100, 101]]
+    assert calls[2][1] == [2.0, 2.0]  # the network's start
+    ramp = np.linspace(-1, 1, 17)
+    rms = lambda c: float(np.sqrt(np.mean((c * ramp) ** 2)))
+    assert abs(out["mlp"]["final_rms_vs_zero_max"] - rms(0.01)) < 1e-12
+    assert abs(out["zero_reseeded"]["final_rms_vs_zero_max"] - rms(0.005)) < 1e-12
+    assert out["zero"]["iters_total"] == 20 and out["mlp"]["converged"] == 2
