@@ -80,11 +80,11 @@ __device__ __forceinline__ void record(uint32_t *histS, unsigned long long *hist
 // histogram: one shared atomic per attempt; `checked` (uniform: the launch
 // can put 2^32 entries into one block's bins) drains a u32 shared bin into
 // the u64 device histogram once it holds 2^31 (the warp-specialised sweep;
-// the windowed sweep flushes all bins between rows instead, flush_hist).  Device (u64) histograms:
-// the entries are merged into runs of equal bins per lane first (E_Delta
-// moves by at most one per attempt, so a window's entries cluster), which
-// saves global atomics; HS = false (weight mode) sends the runs straight to
-// the u64 device histogram.
+// the windowed sweep flushes all bins between rows instead, flush_hist).
+// Device (u64) histograms: the entries are merged into runs of equal bins
+// per lane first (E_Delta moves by at most one per attempt, so a window's
+// entries cluster), which saves global atomics; HS = false (weight mode)
+// sends the runs straight to the u64 device histogram.
 template <int MODE, int SLOTS, bool HS = true>
 __device__ __forceinline__ void record_window(uint32_t *__restrict__ histS, unsigned long long *__restrict__ histG,
                                               const int (&Es)[SLOTS], const int (&Ms)[SLOTS], bool checked)
@@ -377,50 +377,50 @@ __device__ __forceinline__ void scan_window(const WinDec<MODE> &d, bool rec, boo
             }
         }
     } else {
-    WT A = wS[st.E + d.dDel[0]];
-    WT c0 = A, c1 = A;
-    if (SLOTS > 1) {
-        c0 = wS[st.E + d.dDel[1]];
-        c1 = wS[st.E + d.dDel[0] + d.dDel[1]];
-    }
+        WT A = wS[st.E + d.dDel[0]];
+        WT c0 = A, c1 = A;
+        if (SLOTS > 1) {
+            c0 = wS[st.E + d.dDel[1]];
+            c1 = wS[st.E + d.dDel[0] + d.dDel[1]];
+        }
 #pragma unroll
-    for (int t = 0; t < SLOTS; ++t) {
-        WT diff;
-        if (MODE == kModeWeight)
-            diff = __fsub_rn(__fadd_rn((float)d.f2[t], (float)A), (float)wE);
-        else
-            diff = __dsub_rn(__dadd_rn((double)d.f2[t], (double)A), (double)wE);
-        const WT l = (WT)d.lf[t];
-        bool acc;
-        if (ONEBAND) {
-            // logf(u) < 0 for every u <= 1 - 2^-24, so  diff >= 0 || logf(u) < diff
-            // is  logf(u) < diff;  g = __logf(u) - diff has its sign unless |g| <= eps
-            const WT g = l - diff;
-            acc = store && (g < (WT)0);
-            near |= fabs(g) <= eps;
-        } else {
-            // two tests: the one-band form measured 11 % slower in the
-            // single-instance kernel (and 1 % faster in the batch kernel)
-            acc = store && ((diff >= (WT)0) || (l < diff));
-            near |= (diff < (WT)0) && (fabs(l - diff) <= eps);
-        }
-        if (acc) {
-            st.E += d.dDel[t];
-            st.EJ += d.dE[t];
-            st.M += d.dM[t];
-            wE = A;
-            accm |= 0xFu << (4 * t);
-        }
-        Es[t] = st.E;
-        Ms[t] = st.M;
-        if (t + 1 < SLOTS) {
-            A = acc ? c1 : c0;
-            if (t + 2 < SLOTS) {
-                c0 = wS[st.E + d.dDel[t + 2]];
-                c1 = wS[st.E + d.dDel[t + 1] + d.dDel[t + 2]];
+        for (int t = 0; t < SLOTS; ++t) {
+            WT diff;
+            if (MODE == kModeWeight)
+                diff = __fsub_rn(__fadd_rn((float)d.f2[t], (float)A), (float)wE);
+            else
+                diff = __dsub_rn(__dadd_rn((double)d.f2[t], (double)A), (double)wE);
+            const WT l = (WT)d.lf[t];
+            bool acc;
+            if (ONEBAND) {
+                // logf(u) < 0 for every u <= 1 - 2^-24, so  diff >= 0 || logf(u) < diff
+                // is  logf(u) < diff;  g = __logf(u) - diff has its sign unless |g| <= eps
+                const WT g = l - diff;
+                acc = store && (g < (WT)0);
+                near |= fabs(g) <= eps;
+            } else {
+                // two tests: the one-band form measured 11 % slower in the
+                // single-instance kernel (and 1 % faster in the batch kernel)
+                acc = store && ((diff >= (WT)0) || (l < diff));
+                near |= (diff < (WT)0) && (fabs(l - diff) <= eps);
+            }
+            if (acc) {
+                st.E += d.dDel[t];
+                st.EJ += d.dE[t];
+                st.M += d.dM[t];
+                wE = A;
+                accm |= 0xFu << (4 * t);
+            }
+            Es[t] = st.E;
+            Ms[t] = st.M;
+            if (t + 1 < SLOTS) {
+                A = acc ? c1 : c0;
+                if (t + 2 < SLOTS) {
+                    c0 = wS[st.E + d.dDel[t + 2]];
+                    c1 = wS[st.E + d.dDel[t + 1] + d.dDel[t + 2]];
+                }
             }
         }
-    }
     }
     if (__any_sync(0xffffffffu, near)) {
         st = s0;
