@@ -84,3 +84,33 @@ def test_thermalisation_records_nothing(orc):
     rj, rd, _ = orc.energies(L, lat1)
     np.testing.assert_array_equal(ej1, rj)
     np.testing.assert_array_equal(ed1, rd)
+
+
+@pytest.mark.parametrize("program", ["muca_mag", "produce_cpu"])
+def test_cpu_programs_keep_energies_and_counts(orc, program):
+    """The CPU programs' sweeps restated in the oracle (muca_mag.cpp:312-393,
+    random sites with three streams; produce.cpp mcs): one chain per worker,
+    running E_J, E_Delta (and M) equal to the lattice's, one histogram entry
+    per production attempt."""
+    L = 10
+    N = L * L
+    Lb = orc.lib()
+    rng = np.random.default_rng(11)
+    w = np.cumsum(rng.normal(-0.2, 0.8, N + 1))
+    therm, nup = 2 * N + 1, 3 * N + 7
+    for worker in range(3):
+        scheme = orc.scheme_muca_mag(0) if program == "muca_mag" else Lb.orc_scheme_produce_cpu(0)
+        s = orc.init_lattice(L, 1, scheme, chain0=worker).reshape(-1).copy()
+        ej, ed, mg = (np.array([v[0]], np.int32) for v in orc.energies(L, s[None, :]))
+        if program == "muca_mag":
+            h = np.zeros(N + 1, np.uint64)
+            Lb.orc_muca_mag_mcs(L, worker, s, ej, ed, w, h, 2, 100, therm, nup)
+        else:
+            h = np.zeros((N + 1) * (N + 2) // 2, np.uint64)
+            Lb.orc_produce_cpu_mcs(L, worker, s, ej, ed, mg, w, h, 0, 100, therm, nup)
+        rj, rd, rm = orc.energies(L, s[None, :])
+        assert (ej[0], ed[0]) == (rj[0], rd[0])
+        if program == "produce_cpu":
+            assert mg[0] == rm[0]
+        assert int(h.sum()) == nup
+        assert set(np.unique(s)) <= {-1, 0, 1}
