@@ -93,8 +93,9 @@ typedef struct muca_params {
     uint32_t dev_offset; /* index of the first emulated device (a process that runs
                             reference devices k..k+ndev-1 sets k; seeds and init
                             counters follow the device index) */
-    uint32_t kernel;     /* sweep kernel: 0 auto, 1 generic (reference step by step),
-                            2 windowed, 3 warp-specialised (2 and 3 need L % 8 == 0) */
+    uint32_t kernel;     /* sweep kernel: 0 auto (windowed when L % 8 == 0, else generic),
+                            1 generic (reference step by step), 2 windowed,
+                            3 warp-specialised (2 and 3 need L % 8 == 0) */
     uint32_t algorithm;  /* muca_algorithm */
     uint32_t host_logf;  /* random-site algorithm: 1 = the acceptance log is the host libm's logf
                             (what the CPU program computes; bit-exact with it), 0 = CUDA's logf (mcs2) */
