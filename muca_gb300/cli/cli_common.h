@@ -6,7 +6,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstdint>
 #include <cstring>
+#include <fstream>
+#include <iomanip>
 #include <map>
 #include <string>
 #include <sys/stat.h>
@@ -214,6 +217,31 @@ inline void die_chains(const std::string &why)
 }
 
 // ./fss/L<L> is where the reference programs read and write their files.
+// The reference's commented-out histogram output (muca_delta_multigpu.cu:
+// 528-541): one line per E_Delta bin, "i lnW[i] H[i]", lnW with 10
+// significant digits as in the weight files.
+inline bool write_hist_dump(const std::string &path, const std::vector<double> &lnw, const std::vector<uint64_t> &h,
+                            std::string &why)
+{
+    if (lnw.size() != h.size()) {
+        why = path + ": " + std::to_string(lnw.size()) + " weights for " + std::to_string(h.size()) + " bins";
+        return false;
+    }
+    std::ofstream f(path.c_str());
+    if (!f) {
+        why = path + ": cannot be opened for writing";
+        return false;
+    }
+    for (size_t i = 0; i < h.size(); ++i)
+        f << static_cast<int>(i) << " " << std::setprecision(10) << lnw[i] << " " << h[i] << "\n";
+    f.close();
+    if (!f) {
+        why = path + ": write failed";
+        return false;
+    }
+    return true;
+}
+
 inline void ensure_dir(const std::string &d)
 {
     std::string cur;

@@ -65,7 +65,7 @@ int main(int argc, char **argv)
         std::fprintf(stderr,
                      "usage: %s L starting_gpu last_gpu jacks starting_M recursive_update continuing [rand_config]\n"
                      "          [--device=D] [--chains=NW] [--max-iter=K] [--flat=minmean] [--kernel=0..3]\n"
-                     "          [--save-chains=FILE]\n",
+                     "          [--save-chains=FILE] [--hist-dump]\n",
                      argv[0]);
         return 2;
     }
@@ -188,6 +188,19 @@ int main(int argc, char **argv)
             weightfile.close();
         } else {
             std::cout << "Noooo...not converged";
+        }
+        // --hist-dump: the jack's final weights beside its last iteration's
+        // histogram, in the format of the reference's commented-out output
+        // (:528-541), converged or not
+        if (opt.has("hist-dump")) {
+            std::vector<double> lnw((size_t)N + 1);
+            std::vector<uint64_t> hist((size_t)N + 1);
+            if (muca_get_weights(ctx, lnw.data(), N + 1) != MUCA_OK) cli::die("get weights", ctx);
+            if (muca_get_histogram(ctx, hist.data(), N + 1) != MUCA_OK) cli::die("get histogram", ctx);
+            std::string why;
+            if (!cli::write_hist_dump("./fss/L" + Ls + "/E_Delta_multi_T050_JACK" + std::to_string(mm) + ".txt", lnw,
+                                      hist, why))
+                cli::die_io(why);
         }
     }
 

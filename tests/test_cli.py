@@ -447,3 +447,25 @@ def test_weight_run_chains_start_production(exes, orc, tmp_path):
     for (m, s_, _), row in zip(exp, rows):
         assert np.all(np.isfinite(row[1:]))
         np.testing.assert_allclose(row[1:], [m[0], m[1], s_[0], s_[1]], rtol=2e-9, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_multigpu_weight_hist_dump(exes, tmp_path):
+    """--hist-dump writes each jack's final weights beside its last
+    iteration's histogram, in the reference's commented-out format
+    (muca_delta_multigpu.cu:528-541): the weights equal the weight file's,
+    and every chain contributed the same number of entries."""
+    L, NW = 4, 256
+    N = L * L
+    r = subprocess.run([exes[0], str(L), "0", "0", "1", "1", "0", "0", "--chains=%d" % NW, "--max-iter=3000",
+                        "--hist-dump"], capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stderr
+    d = tmp_path / "fss" / ("L%d" % L)
+    rows = [ln.split(" ") for ln in (d / "E_Delta_multi_T050_JACK0.txt").read_text().splitlines()]
+    assert [int(x[0]) for x in rows] == list(range(N + 1))
+    h = np.array([int(x[2]) for x in rows], np.uint64)
+    assert int(h.sum()) > 0 and int(h.sum()) % NW == 0
+    wfiles = [f for f in os.listdir(d) if f.startswith("weight_gpu1_")]
+    if wfiles:  # written on convergence, from the same final weights
+        wrows = [ln.split(" ") for ln in (d / wfiles[0]).read_text().splitlines()]
+        assert [x[1] for x in rows] == [x[1] for x in wrows]
